@@ -1,0 +1,323 @@
+#!/usr/bin/env python3
+"""Benchmark of the constellation DFS hot path on GB300 (one JSON line).
+
+Workload: the plain single-N count at N=19 -- all 897,071 tasks of the
+reference's preset-6 constellation set (4,968,057,848 solutions) -- one launch
+sequence (prepare + DFS) per step.  metric = DFS nodes/s, where a node is one
+candidate-queen extraction of the reference's dfs_iter
+(14Bit_codon_GPU/356Py_savesp_narrow.py:1904-1965) and the per-N node totals
+are frozen constants counted once by the CPU oracle (DFS_NODES below).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+value: inputs resident in HBM, device-timed (CUDA events on the launching
+stream), L2 flushed (256 MiB write) between timed steps.  e2e: the same
+metric through the C ABI call nq_exec_solutions with pinned host records,
+host->device copy and device->host read-back inside the timed region.
+--impl reference: the reference algorithm's CPU implementation on the host
+cores (the C oracle port, all threads) on a bounded seeded sample of the same
+workload.  Multi-GPU: one process per GPU (torchrun), each rank counts the
+full N=19 workload (replicas, weak scaling); value = all ranks' nodes / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+for _p in (os.path.join(REPO, "n-queens_gb300"), os.path.join(REPO, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+# DFS nodes per N at the reference's dynamic preset (select_dynamic_preset_queens), counted by
+# oracle.exec_solutions(N, oracle.gen_constellations(N, preset), want_nodes=True).
+DFS_NODES = {10: 4980, 11: 27032, 12: 145880, 13: 787610, 14: 4578224, 15: 27864613, 16: 182533515,
+             17: 1247485360, 18: 9087554384, 19: 69276398858}
+N_BENCH = 19
+OPS_PER_NODE = 12   # INT32 ops per node in the reference hot loop (neg, and, xor, or, shl, or, shr, or, or, or, andnot, cmp)
+METRIC = "N=19 DFS nodes/s"
+
+
+def load_peaks():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return json.load(f)
+    except OSError:
+        return None
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = os.path.join(REPO, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sms, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sms.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sms) if sms else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sms)}
+
+
+def cpu_sample(N: int, frac: float, seed: int):
+    """Seeded subset of the N-workload's records for the CPU legs."""
+    import numpy as np
+    import nqueens
+    import oracle
+    recs = nqueens.gen_records(N)
+    rng = np.random.default_rng(seed)
+    take = max(1, int(round(frac * len(recs))))
+    idx = np.sort(rng.choice(len(recs), size=take, replace=False))
+    sub = recs[idx]
+    return oracle.Records(sub["ld"].astype(np.uint64), sub["rd"].astype(np.uint64), sub["col"].astype(np.uint64),
+                          sub["startijkl"].copy()), len(recs)
+
+
+def run_cpu(N: int, target_s: float, seed: int = 2026):
+    """Oracle port on all host threads over a sample sized to ~target_s seconds; returns nodes/s etc."""
+    import oracle
+    oracle.build()
+    threads = os.cpu_count() or 1
+    # calibrate on a small slice, then size the sample
+    rec, m_all = cpu_sample(N, 1 / 512, seed)
+    t0 = time.perf_counter()
+    _, nodes = oracle.exec_solutions(N, rec, threads=threads, want_nodes=True)
+    dt = max(time.perf_counter() - t0, 1e-3)
+    rate = float(nodes.sum()) / dt
+    frac = min(1.0, max(1 / 512, target_s * rate / DFS_NODES[N]))
+    rec, m_all = cpu_sample(N, frac, seed + 1)
+    t0 = time.perf_counter()
+    _, nodes = oracle.exec_solutions(N, rec, threads=threads, want_nodes=True)
+    dt = time.perf_counter() - t0
+    n = int(nodes.sum())
+    return {"value": n / dt, "nodes": n, "seconds": dt, "cores": threads, "tasks": len(rec), "tasks_all": m_all,
+            "frac": frac}
+
+
+def reference_arm(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    steps = []
+    for _ in range(args.warmup):
+        run_cpu(N_BENCH, 2.0)
+    for _ in range(args.steps):
+        steps.append(run_cpu(N_BENCH, args.cpu_seconds))
+    vals = [s["value"] for s in steps]
+    v = statistics.mean(vals)
+    s0 = steps[0]
+    sample = (f"seeded {s0['frac']:.4f} of the N=19 preset-6 task list ({s0['tasks']} of {s0['tasks_all']} tasks, "
+              f"~{s0['seconds']:.1f} s per step), nodes from the oracle's own dfs_iter counter")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "nodes/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(s["seconds"] for s in steps),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": "plain single-N count, N=19, preset 6 (897,071 tasks), CPU sample",
+                   "N": N_BENCH, "preset": 6},
+        "cpu_baseline": {"value": v, "unit": "nodes/s", "cores": s0["cores"], "kind": "port", "sample": sample},
+        "e2e": {"value": v, "unit": "nodes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": ("CPU implementation of the reference algorithm (C restatement of 356Py dfs_iter + generator, "
+                 "oracle/nq_oracle.c, pthreads); the reference's own C port (10Bit_CUDA/13CUDA_constellation.c) "
+                 "is built from the reference checkout, which the GPU host does not have"),
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def read_traffic():
+    """dram bytes per dfs_kernel launch from the committed ncu summary, or None."""
+    p = os.path.join(REPO, "profiles", "dfs_kernel_n19_traffic.txt")
+    try:
+        for line in open(p):
+            if line.startswith("dram_bytes_per_launch:"):
+                return float(line.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
+def ours_arm(args):
+    import numpy as np
+    import torch
+    import nqueens
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = local if ws > 1 else 0
+    torch.cuda.set_device(dev)
+    eng = nqueens.Engine(dev, block=args.block)
+    N = N_BENCH
+    expected = 4968057848
+    recs = nqueens.gen_records(N)
+    m = len(recs)
+    start_min = int((recs["startijkl"] >> 20).min())
+    d_rec = torch.from_numpy(recs.view(np.uint8).copy()).to(f"cuda:{dev}")
+    d_total = torch.zeros(1, dtype=torch.int64, device=f"cuda:{dev}")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{dev}")
+    s = torch.cuda.Stream(device=dev)
+
+    def step():
+        eng.exec_device(N, d_rec.data_ptr(), m, start_min, d_total.data_ptr(), 0, s.cuda_stream)
+
+    for _ in range(args.warmup):
+        step()
+        eng.sync()
+        assert int(d_total.item()) == expected, "N=19 total mismatch"
+    peaks = load_peaks()
+    int_peak = eng.int32_peak(0)
+    int_peak_add = eng.int32_peak(1)
+
+    clocks = Clocks(dev)
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    dfs_ms = []
+    for i in range(args.steps):
+        with torch.cuda.stream(s):
+            flush.zero_()                      # L2 flush (256 MiB > 129 MB L2), outside the timed events
+            ev[i][0].record(s)
+        step()
+        with torch.cuda.stream(s):
+            ev[i][1].record(s)
+        eng.sync()
+        dfs_ms.append(eng.last_kernel_ms()[1])
+        assert int(d_total.item()) == expected
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    t_ms = sum(step_ms)
+    if ws > 1:
+        t = torch.tensor([t_ms], device=f"cuda:{dev}", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_ms = float(t.item())
+    ms_per_step = t_ms / args.steps
+    nodes = DFS_NODES[N]
+    value = ws * nodes * args.steps / (t_ms * 1e-3)
+
+    # e2e: host records (pinned) -> C ABI -> host total
+    pinned = torch.empty(m * 16, dtype=torch.uint8, pin_memory=True)
+    pinned.numpy()[:] = recs.view(np.uint8)
+    h_recs = pinned.numpy().view(nqueens.RECORD_DTYPE)
+    e2e_t = []
+    for i in range(args.steps + 1):
+        flush.zero_(); torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        tot, _ = eng.exec_records(N, h_recs)
+        e2e_t.append(time.perf_counter() - t0)
+        assert tot == expected
+    e2e_s = statistics.mean(e2e_t[1:])
+    # the reference's "wall s per N": generation + upload + count + read-back through nq_count
+    t0 = time.perf_counter()
+    assert eng.count(N).total == expected
+    wall_n19 = time.perf_counter() - t0
+
+    dfs_avg = statistics.mean(dfs_ms)
+    achieved_ops = nodes * OPS_PER_NODE / (dfs_avg * 1e-3)
+    traffic = read_traffic()
+    line = {
+        "metric": METRIC, "value": value, "unit": "nodes/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": "plain single-N count, N=19, preset 6 (897,071 tasks, 4,968,057,848 solutions), "
+                               "one prepare+DFS launch pair per step",
+                   "N": N, "preset": 6, "tasks": m, "block": args.block,
+                   "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{ws}"},
+        "n19_total": expected,
+        "n19_wall_s": wall_n19,
+        "dfs_kernel_ms": dfs_avg,
+        "e2e": {"value": ws * nodes / e2e_s, "unit": "nodes/s", "seconds_per_step": e2e_s,
+                "h2d_bytes_per_step": m * 16, "d2h_bytes_per_step": 16},
+        "roofline": {"bound": "alu", "achieved": achieved_ops / 1e9, "peak": int_peak / 1e9, "unit": "Gop/s",
+                     "frac": achieved_ops / int_peak, "traffic": traffic,
+                     "peak_source": "measured in this run: lop3.b32 throughput probe (nq_int32_peak); "
+                                    f"add.u32 probe {int_peak_add / 1e9:.0f} Gop/s",
+                     "ops_per_node": OPS_PER_NODE,
+                     "hbm_frac": (m * 16 + m * 16 + m * 8 + m * 4 * 15) / (dfs_avg * 1e-3) / (
+                         (peaks or {}).get("hbm_gbs", 6800.0) * 1e9)},
+        "clocks": clk,
+        "gpu_launches": 2 * args.steps,
+    }
+    if rank == 0 and not args.no_cpu:
+        cb = run_cpu(N, args.cpu_seconds)
+        line["cpu_baseline"] = {"value": cb["value"], "unit": "nodes/s", "cores": cb["cores"], "kind": "port",
+                                "sample": (f"seeded {cb['frac']:.4f} of the N=19 task list ({cb['tasks']} tasks, "
+                                           f"{cb['seconds']:.1f} s), C oracle port, all host threads")}
+    if rank == 0:
+        print(json.dumps(line))
+    eng.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--block", type=int, default=128)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return reference_arm(args)
+    return ours_arm(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

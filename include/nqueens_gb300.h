@@ -1,0 +1,148 @@
+/*
+ * nqueens_gb300.h -- C ABI of libnqgpu.so, the GB300 (sm_103a) N-Queens
+ * constellation engine.
+ *
+ * Plain C types only (no torch, no C++): bind it from ctypes, cgo, JNI or
+ * C/C++.  Every function that can fail returns an int status: NQ_OK (0) or a
+ * negative NQ_E* code; nq_last_error() gives the message of the handle's last
+ * failure.  A device-side failure is always an error status, never a partial
+ * count.
+ *
+ * Each declaration names the reference interface it replaces, by file:line in
+ * suzukiiichiro/N-Queens.
+ */
+#ifndef NQUEENS_GB300_H
+#define NQUEENS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NQ_OK 0
+#define NQ_EINVAL (-1)     /* bad argument */
+#define NQ_ESTACK (-2)     /* a task is deeper than the launch's stack (never a partial count) */
+#define NQ_ETIMEOUT (-3)   /* a bounded wait ran out */
+#define NQ_ECUDA (-4)      /* CUDA runtime error (message in nq_last_error) */
+#define NQ_ENOMEM (-5)     /* device or host allocation failed */
+#define NQ_EPRESET (-6)    /* preset too deep for N: the reference raises on the negative shift */
+#define NQ_EBUSY (-7)      /* asynchronous work still running */
+
+/* The reference's 16-byte task record, little-endian u32 fields, exactly the
+ * layout of its constellations_N{N}_{P}.bin files
+ * (14Bit_codon_GPU/356Py_savesp_narrow.py:2981-2986). */
+typedef struct nq_record {
+  uint32_t ld, rd, col, startijkl;
+} nq_record;
+
+typedef struct nq_handle nq_handle;
+
+const char *nq_version(void);
+const char *nq_strerror(int status);
+
+/* One handle = one device + one CUDA stream.  Calls on a handle are
+ * serialised by the caller; different handles are independent. */
+int nq_create(nq_handle **out, int device);
+void nq_destroy(nq_handle *h);
+int nq_last_error(const nq_handle *h, char *buf, size_t cap);
+
+/* Launch knobs chosen by the autotuner: threads per block (64, 128 or 256),
+ * grid (0 = one wave of resident blocks) and queue order (0 = record order,
+ * 1 = estimated cost, largest first). */
+int nq_set_config(nq_handle *h, int block, int grid, int order_mode);
+int nq_get_config(const nq_handle *h, int *block, int *grid, int *order_mode);
+
+/* select_dynamic_preset_queens (356Py_savesp_narrow.py:5744-5753). */
+int nq_preset_for(int N);
+
+/* gen_constellations (356Py_savesp_narrow.py:2837-2926) on the host: writes
+ * up to `cap` records and returns the total count (call with cap = 0 to size
+ * the buffer), or a negative status.  5 <= N <= 27. */
+int64_t nq_gen_constellations(int N, int preset, nq_record *out, int64_t cap);
+/* Same records with the reference's full-width masks (Python ints there),
+ * as its 40-byte solutions_*_v2.bin files store them
+ * (13Bit_codon/18Py_constellations_GPU_cuda_codon.py:1841-1855). */
+int64_t nq_gen_constellations_wide(int N, int preset, uint64_t *ld, uint64_t *rd, uint64_t *col,
+                                   uint32_t *startijkl, int64_t cap);
+
+/* exec_solutions(N, constellations, use_gpu=True)
+ * (356Py_savesp_narrow.py:2228-2578, kernel launch :1749-1835): host records
+ * in, host results out.  `solutions` (nullable) receives each record's count
+ * times its symmetry weight (the reference's c["solutions"]); `total`
+ * receives their sum.  6 <= N <= 27. */
+int nq_exec_solutions(nq_handle *h, int N, const nq_record *records, int64_t m, uint64_t *solutions,
+                      uint64_t *total);
+
+/* Same on device-resident buffers, asynchronous on `stream` (NULL: the
+ * handle's stream).  `start_min` is the smallest start row
+ * (startijkl >> 20) over the records, or -1 to use the bound 1.
+ * d_total (device, 1 x u64) is overwritten.  Call nq_sync() to wait and
+ * collect the status. */
+int nq_exec_solutions_device(nq_handle *h, int N, const nq_record *d_records, int64_t m, int start_min,
+                             uint64_t *d_solutions, uint64_t *d_total, void *stream);
+int nq_sync(nq_handle *h);
+/* Device time of the last exec_solutions call's prepare and DFS kernels
+ * (CUDA events recorded on the launching stream); waits for them. */
+int nq_last_kernel_ms(nq_handle *h, float *prepare_ms, float *dfs_ms);
+
+/* Whole-board total for N, the loop body of the reference's main()
+ * (356Py_savesp_narrow.py:6036-6046): brute force on the GPU for N <= 5
+ * (the reference's _bit_total, :5755-5767), the constellation path above.
+ * preset <= 0 selects nq_preset_for(N). */
+int nq_count(nq_handle *h, int N, int preset, uint64_t *total);
+
+/* Completions of a board with k pre-placed queens (rows[i], cols[i]; column c
+ * is bit c): the number of full placements that contain them.  No reference
+ * counterpart (the reference counts whole boards only); brute-force checked. */
+int nq_count_completions(nq_handle *h, int N, int k, const int *rows, const int *cols, uint64_t *count);
+
+/* Diagnostic: the root frame {ld, rd, col, avail}, info word and compact
+ * per-depth schedule words that the prepare kernel derives from one record
+ * (build_soa_for_range, 356Py_savesp_narrow.py:1971-2169, plus the SQ* walk
+ * of :689-756), computed by the same code on the host.  Returns the number
+ * of words (T+1), 0 for a task without DFS work, or a negative status. */
+int nq_debug_task_schedule(int N, nq_record rec, uint32_t root[4], uint32_t *info, uint32_t *words, int cap);
+
+/* Diagnostic: the host-built tasks of a completion query (see
+ * nq_count_completions), wide format: per task root {ld, rd, col, avail},
+ * info word and (T+1) word pairs {x, RA} at words + task * 2 * stride.
+ * Returns the task count (call with cap = 0 to size), or a negative status. */
+int64_t nq_debug_completion_tasks(int N, int k, const int *rows, const int *cols, int min_tasks,
+                                  uint32_t *roots, uint32_t *infos, uint32_t *words, int stride, int64_t cap);
+
+/* Diagnostic: measured INT32 instruction throughput of the device (thread
+ * instructions per second) for kind 0 = lop3, 1 = add, 2 = shf, 3 = a 1:1:1
+ * mix; the denominator of the DFS kernel's integer-ALU roofline. */
+int nq_int32_peak(nq_handle *h, int kind, double *ops_per_s);
+
+/* ---- batches: many jobs in one persistent launch ---- */
+#define NQ_JOB_COUNT 0        /* whole-board total of N (preset 0 = nq_preset_for) */
+#define NQ_JOB_COMPLETION 1   /* completions of the k pre-placed queens */
+typedef struct nq_job {
+  int32_t kind, N, preset, k;
+  int8_t rows[8], cols[8];
+} nq_job;
+
+typedef struct nq_batch nq_batch;
+
+/* Builds every job's tasks, uploads them once and keeps them resident. */
+int nq_batch_create(nq_handle *h, const nq_job *jobs, int njobs, nq_batch **out);
+int64_t nq_batch_tasks(const nq_batch *b);
+int64_t nq_batch_device_bytes(const nq_batch *b);
+/* All jobs in one persistent launch (use_graph: replay a captured CUDA graph). */
+int nq_batch_run(nq_batch *b, int use_graph, uint64_t *totals);
+/* One launch and one read-back per job (the plain form, for comparison). */
+int nq_batch_run_plain(nq_batch *b, uint64_t *totals);
+/* Asynchronous form on the batch's own stream, so batches overlap on the
+ * device: submit, then poll (waits up to max_wait_us; NQ_EBUSY while
+ * running). */
+int nq_batch_submit(nq_batch *b, int use_graph);
+int nq_batch_poll(nq_batch *b, uint64_t *totals, int64_t max_wait_us);
+void nq_batch_destroy(nq_batch *b);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NQUEENS_GB300_H */

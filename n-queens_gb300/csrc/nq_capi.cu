@@ -1,0 +1,679 @@
+// nq_capi.cu -- the extern "C" boundary of libnqgpu.so (include/nqueens_gb300.h).
+//
+// Owns device memory, streams, error reporting and the launch sequence:
+//   records (host or device) -> prepare_kernel -> dfs_kernel -> totals.
+// The library has no CPU counting path: every count is computed by the
+// kernels in nq_kernels.cu.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/nqueens_gb300.h"
+#include "nq_common.cuh"
+#include "nq_host.h"
+#include "nq_internal.h"
+
+using namespace nq;
+
+namespace {
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  cudaError_t ensure(size_t n) {
+    if (n <= cap) return cudaSuccess;
+    if (p) { cudaFree(p); p = nullptr; cap = 0; }
+    size_t want = std::max<size_t>(n, 256);
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e == cudaSuccess) cap = want;
+    return e;
+  }
+  void release() { if (p) cudaFree(p); p = nullptr; cap = 0; }
+};
+
+// Control block of one run: totals (u64 per job), queue cursor, error word.
+struct Ctrl {
+  static size_t bytes(int njobs) { return (size_t)njobs * 8 + 16; }
+};
+
+int preset_for(int N) {
+  if (N >= 5 && N <= 17) return 5;
+  if (N >= 18 && N <= 21) return 6;
+  if (N >= 22 && N <= 24) return 7;
+  if (N >= 25 && N <= 27) return 8;
+  return 5;
+}
+
+int derr_to_status(uint32_t e) {
+  if (e & DERR_DEPTH) return NQ_ESTACK;
+  if (e & DERR_SHIFT) return NQ_EPRESET;
+  if (e) return NQ_EINVAL;
+  return NQ_OK;
+}
+
+const char* derr_text(uint32_t e) {
+  if (e & DERR_DEPTH) return "a task's schedule is deeper than the launch's stack";
+  if (e & DERR_SHIFT) return "a record needs a negative shift (preset too deep for N)";
+  if (e & DERR_NOTERM) return "a task's schedule never reaches a base frame";
+  if (e & DERR_BADN) return "task with N outside 6..27";
+  return "ok";
+}
+
+int maxt_for(int N, int start_min) {
+  // Terminal-parent depth T <= N - 3 - start; one frame of margin.
+  int s = start_min < 0 ? 1 : start_min;
+  int m = N - 2 - s;
+  return std::max(1, std::min(m, kMaxDepth - 1));
+}
+
+}  // namespace
+
+struct nq_handle {
+  int device = 0;
+  int sms = 0;
+  cudaStream_t stream = nullptr;
+  int block = 128, grid = 0, order_mode = 0;
+  std::string err;
+  DevBuf rec, root, info, sched, per_task, ctrl;
+  uint64_t* h_ctrl = nullptr;   // pinned read-back of the control block
+  size_t h_ctrl_cap = 0;
+  bool pending = false;
+  // events around the last run's kernels (same stream as the launches)
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+
+  int fail(int status, const char* fmt, ...) {
+    char buf[512];
+    va_list ap; va_start(ap, fmt); vsnprintf(buf, sizeof buf, fmt, ap); va_end(ap);
+    err = buf;
+    return status;
+  }
+  int cuda_fail(cudaError_t e, const char* where) {
+    return fail(e == cudaErrorMemoryAllocation ? NQ_ENOMEM : NQ_ECUDA, "%s: %s", where, cudaGetErrorString(e));
+  }
+  int ensure_pinned(size_t bytes) {
+    if (bytes <= h_ctrl_cap) return NQ_OK;
+    if (h_ctrl) cudaFreeHost(h_ctrl);
+    h_ctrl = nullptr; h_ctrl_cap = 0;
+    cudaError_t e = cudaMallocHost((void**)&h_ctrl, bytes);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMallocHost");
+    h_ctrl_cap = bytes;
+    return NQ_OK;
+  }
+};
+
+#define NQ_CUDA(h, call)                                     \
+  do {                                                       \
+    cudaError_t _e = (call);                                 \
+    if (_e != cudaSuccess) return (h)->cuda_fail(_e, #call); \
+  } while (0)
+
+namespace {
+
+// records (device) -> counts.  Asynchronous on st; totals land in ctrl[0].
+int run_records(nq_handle* h, int N, const uint4* d_rec, int64_t m, int start_min, unsigned long long* d_per_task,
+                cudaStream_t st) {
+  const int maxt = maxt_for(N, start_min);
+  const int sw = maxt + 1;
+  NQ_CUDA(h, cudaSetDevice(h->device));
+  NQ_CUDA(h, h->root.ensure((size_t)m * sizeof(uint4)));
+  NQ_CUDA(h, h->info.ensure((size_t)m * sizeof(uint2)));
+  NQ_CUDA(h, h->sched.ensure((size_t)m * sw * sizeof(uint32_t)));
+  NQ_CUDA(h, h->ctrl.ensure(Ctrl::bytes(1)));
+  unsigned char* c = (unsigned char*)h->ctrl.p;
+  NQ_CUDA(h, cudaMemsetAsync(c, 0, Ctrl::bytes(1), st));
+  TaskArrays ta;
+  ta.root = (uint4*)h->root.p; ta.info = (uint2*)h->info.p; ta.sched = h->sched.p; ta.sw = sw; ta.wide = false;
+  unsigned int* cursor = (unsigned int*)(c + 8);
+  unsigned int* err = (unsigned int*)(c + 12);
+  NQ_CUDA(h, cudaEventRecord(h->ev[0], st));
+  NQ_CUDA(h, launch_prepare(N, m, d_rec, ta, 0, 0, err, st));
+  NQ_CUDA(h, cudaEventRecord(h->ev[1], st));
+  DfsLaunch L;
+  L.tasks = ta; L.m = m; L.order = nullptr; L.cursor = cursor; L.job_totals = (unsigned long long*)c;
+  L.per_task = d_per_task; L.err = err; L.maxt = maxt; L.block = h->block; L.grid = h->grid;
+  NQ_CUDA(h, launch_dfs(L, st));
+  NQ_CUDA(h, cudaEventRecord(h->ev[2], st));
+  return NQ_OK;
+}
+
+int read_ctrl(nq_handle* h, cudaStream_t st, uint64_t* total) {
+  if (int s = h->ensure_pinned(Ctrl::bytes(1))) return s;
+  NQ_CUDA(h, cudaMemcpyAsync(h->h_ctrl, h->ctrl.p, Ctrl::bytes(1), cudaMemcpyDeviceToHost, st));
+  NQ_CUDA(h, cudaStreamSynchronize(st));
+  const uint32_t e = ((const uint32_t*)h->h_ctrl)[3];
+  if (e) return h->fail(derr_to_status(e), "device: %s", derr_text(e));
+  if (total) *total = h->h_ctrl[0];
+  return NQ_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+extern "C" {
+
+const char* nq_version(void) { return "nqueens-gb300 0.1 (sm_103a)"; }
+
+const char* nq_strerror(int s) {
+  switch (s) {
+    case NQ_OK: return "ok";
+    case NQ_EINVAL: return "invalid argument";
+    case NQ_ESTACK: return "task deeper than the launch's stack";
+    case NQ_ETIMEOUT: return "bounded wait ran out";
+    case NQ_ECUDA: return "CUDA error";
+    case NQ_ENOMEM: return "out of memory";
+    case NQ_EPRESET: return "preset too deep for N";
+    case NQ_EBUSY: return "still running";
+    default: return "unknown status";
+  }
+}
+
+int nq_create(nq_handle** out, int device) {
+  if (!out) return NQ_EINVAL;
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) return NQ_ECUDA;
+  nq_handle* h = new (std::nothrow) nq_handle();
+  if (!h) return NQ_ENOMEM;
+  h->device = device;
+  if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
+      cudaEventCreate(&h->ev[0]) != cudaSuccess || cudaEventCreate(&h->ev[1]) != cudaSuccess ||
+      cudaEventCreate(&h->ev[2]) != cudaSuccess) {
+    nq_destroy(h);
+    return NQ_ECUDA;
+  }
+  *out = h;
+  return NQ_OK;
+}
+
+void nq_destroy(nq_handle* h) {
+  if (!h) return;
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  h->rec.release(); h->root.release(); h->info.release(); h->sched.release(); h->per_task.release(); h->ctrl.release();
+  if (h->h_ctrl) cudaFreeHost(h->h_ctrl);
+  for (auto& e : h->ev) if (e) cudaEventDestroy(e);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+}
+
+int nq_int32_peak(nq_handle* h, int kind, double* ops_per_s) {
+  if (!h || !ops_per_s || kind < 0 || kind > 3) return NQ_EINVAL;
+  NQ_CUDA(h, cudaSetDevice(h->device));
+  NQ_CUDA(h, h->ctrl.ensure(Ctrl::bytes(1)));
+  int per = 0;
+  NQ_CUDA(h, cudaDeviceGetAttribute(&per, cudaDevAttrMaxThreadsPerMultiProcessor, h->device));
+  const int grid = h->sms * std::max(1, per / 256);
+  const int iters = 4096;
+  cudaStream_t st = h->stream;
+  NQ_CUDA(h, int_peak(kind, 64, grid, (uint32_t*)h->ctrl.p, st));   // warm-up
+  double best = 0.0;
+  for (int rep = 0; rep < 3; rep++) {
+    NQ_CUDA(h, cudaEventRecord(h->ev[0], st));
+    NQ_CUDA(h, int_peak(kind, iters, grid, (uint32_t*)h->ctrl.p, st));
+    NQ_CUDA(h, cudaEventRecord(h->ev[1], st));
+    NQ_CUDA(h, cudaEventSynchronize(h->ev[1]));
+    float ms = 0.f;
+    NQ_CUDA(h, cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]));
+    const double ops = (double)grid * 256.0 * (double)iters * 128.0;
+    best = std::max(best, ops / (ms * 1e-3));
+  }
+  *ops_per_s = best;
+  return NQ_OK;
+}
+
+int nq_last_kernel_ms(nq_handle* h, float* prepare_ms, float* dfs_ms) {
+  if (!h) return NQ_EINVAL;
+  NQ_CUDA(h, cudaSetDevice(h->device));
+  NQ_CUDA(h, cudaEventSynchronize(h->ev[2]));
+  float a = 0.f, b = 0.f;
+  NQ_CUDA(h, cudaEventElapsedTime(&a, h->ev[0], h->ev[1]));
+  NQ_CUDA(h, cudaEventElapsedTime(&b, h->ev[1], h->ev[2]));
+  if (prepare_ms) *prepare_ms = a;
+  if (dfs_ms) *dfs_ms = b;
+  return NQ_OK;
+}
+
+int nq_last_error(const nq_handle* h, char* buf, size_t cap) {
+  if (!h || !buf || cap == 0) return NQ_EINVAL;
+  snprintf(buf, cap, "%s", h->err.c_str());
+  return NQ_OK;
+}
+
+int nq_set_config(nq_handle* h, int block, int grid, int order_mode) {
+  if (!h) return NQ_EINVAL;
+  if (block != 64 && block != 128 && block != 256) return h->fail(NQ_EINVAL, "block must be 64, 128 or 256");
+  if (grid < 0 || order_mode < 0 || order_mode > 1) return h->fail(NQ_EINVAL, "bad grid or order mode");
+  h->block = block; h->grid = grid; h->order_mode = order_mode;
+  return NQ_OK;
+}
+
+int nq_get_config(const nq_handle* h, int* block, int* grid, int* order_mode) {
+  if (!h) return NQ_EINVAL;
+  if (block) *block = h->block;
+  if (grid) *grid = h->grid;
+  if (order_mode) *order_mode = h->order_mode;
+  return NQ_OK;
+}
+
+int nq_preset_for(int N) { return preset_for(N); }
+
+int64_t nq_gen_constellations(int N, int preset, nq_record* out, int64_t cap) {
+  std::vector<GenRecord> v;
+  const int s = gen_constellations(N, preset, v, 0);
+  if (s == -1) return NQ_EINVAL;
+  if (s == -2) return NQ_EPRESET;
+  const int64_t n = (int64_t)v.size();
+  if (out && cap >= n)
+    for (int64_t i = 0; i < n; i++)
+      out[i] = nq_record{(uint32_t)v[i].ld, (uint32_t)v[i].rd, (uint32_t)v[i].col, v[i].startijkl};
+  return n;
+}
+
+int64_t nq_gen_constellations_wide(int N, int preset, uint64_t* ld, uint64_t* rd, uint64_t* col, uint32_t* sijkl,
+                                   int64_t cap) {
+  std::vector<GenRecord> v;
+  const int s = gen_constellations(N, preset, v, 0);
+  if (s == -1) return NQ_EINVAL;
+  if (s == -2) return NQ_EPRESET;
+  const int64_t n = (int64_t)v.size();
+  if (ld && rd && col && sijkl && cap >= n)
+    for (int64_t i = 0; i < n; i++) { ld[i] = v[i].ld; rd[i] = v[i].rd; col[i] = v[i].col; sijkl[i] = v[i].startijkl; }
+  return n;
+}
+
+int nq_exec_solutions(nq_handle* h, int N, const nq_record* records, int64_t m, uint64_t* solutions, uint64_t* total) {
+  if (!h || !total || m < 0 || (m > 0 && !records)) return h ? h->fail(NQ_EINVAL, "null argument") : NQ_EINVAL;
+  if (N < 6 || N > kMaxN) return h->fail(NQ_EINVAL, "exec_solutions: N=%d outside 6..27", N);
+  if (m > (int64_t)0x7FFFFFFF) return h->fail(NQ_EINVAL, "too many records");
+  *total = 0;
+  if (m == 0) return NQ_OK;
+  cudaStream_t st = h->stream;
+  NQ_CUDA(h, cudaSetDevice(h->device));
+  const int smin = (int)start_row_min(&records[0].startijkl, m, 4);
+  NQ_CUDA(h, h->rec.ensure((size_t)m * sizeof(nq_record)));
+  NQ_CUDA(h, cudaMemcpyAsync(h->rec.p, records, (size_t)m * sizeof(nq_record), cudaMemcpyHostToDevice, st));
+  unsigned long long* pt = nullptr;
+  if (solutions) {
+    NQ_CUDA(h, h->per_task.ensure((size_t)m * 8));
+    pt = (unsigned long long*)h->per_task.p;
+  }
+  if (int s = run_records(h, N, (const uint4*)h->rec.p, m, smin, pt, st)) return s;
+  if (solutions) NQ_CUDA(h, cudaMemcpyAsync(solutions, pt, (size_t)m * 8, cudaMemcpyDeviceToHost, st));
+  return read_ctrl(h, st, total);
+}
+
+int nq_exec_solutions_device(nq_handle* h, int N, const nq_record* d_records, int64_t m, int start_min,
+                             uint64_t* d_solutions, uint64_t* d_total, void* stream) {
+  if (!h || !d_total || m < 0 || (m > 0 && !d_records)) return h ? h->fail(NQ_EINVAL, "null argument") : NQ_EINVAL;
+  if (N < 6 || N > kMaxN) return h->fail(NQ_EINVAL, "exec_solutions: N=%d outside 6..27", N);
+  if (m > (int64_t)0x7FFFFFFF) return h->fail(NQ_EINVAL, "too many records");
+  cudaStream_t st = stream ? (cudaStream_t)stream : h->stream;
+  NQ_CUDA(h, cudaSetDevice(h->device));
+  if (m == 0) {
+    NQ_CUDA(h, cudaMemsetAsync(d_total, 0, 8, st));
+    return NQ_OK;
+  }
+  if (int s = run_records(h, N, (const uint4*)d_records, m, start_min, (unsigned long long*)d_solutions, st)) return s;
+  NQ_CUDA(h, cudaMemcpyAsync(d_total, h->ctrl.p, 8, cudaMemcpyDeviceToDevice, st));
+  h->pending = true;
+  return NQ_OK;
+}
+
+int nq_sync(nq_handle* h) {
+  if (!h) return NQ_EINVAL;
+  NQ_CUDA(h, cudaSetDevice(h->device));
+  NQ_CUDA(h, cudaDeviceSynchronize());
+  if (!h->pending) return NQ_OK;
+  h->pending = false;
+  uint32_t e = 0;
+  NQ_CUDA(h, cudaMemcpy(&e, (unsigned char*)h->ctrl.p + 12, 4, cudaMemcpyDeviceToHost));
+  if (e) return h->fail(derr_to_status(e), "device: %s", derr_text(e));
+  return NQ_OK;
+}
+
+int nq_debug_task_schedule(int N, nq_record rec, uint32_t root[4], uint32_t* info, uint32_t* words, int cap) {
+  if (N < 6 || N > kMaxN || !root || !info || (cap > 0 && !words) || cap < 0) return NQ_EINVAL;
+  const TaskHead t = decode_record(N, rec.ld, rec.rd, rec.col, rec.startijkl);
+  if (t.status != TS_OK) return NQ_EPRESET;
+  Root rt;
+  uint32_t rc = 0;
+  Op ops[kMaxDepth];
+  const int T = walk_schedule(N, t, &rt, &rc, ops, std::min(cap, kMaxDepth));
+  if (T == -2) return NQ_ESTACK;
+  root[0] = rt.ld; root[1] = rt.rd; root[2] = rt.col; root[3] = (T < 0) ? 0u : rt.avail;
+  *info = info_pack(T < 0 ? INFO_NO_DFS : (uint32_t)T, (uint32_t)t.wexp, rc, (uint32_t)N, TS_OK);
+  if (T < 0) return 0;
+  for (int d = 0; d <= T; d++) words[d] = pack_compact(ops[d]);
+  return T + 1;
+}
+
+int64_t nq_debug_completion_tasks(int N, int k, const int* rows, const int* cols, int min_tasks, uint32_t* roots,
+                                  uint32_t* infos, uint32_t* words, int stride, int64_t cap) {
+  if (k < 0 || k > 8 || (k > 0 && (!rows || !cols)) || stride < 1) return NQ_EINVAL;
+  std::vector<HostTask> v;
+  int mt = 0;
+  const int s = build_completion_tasks(N, k, rows, cols, min_tasks, 0, v, &mt);
+  if (s < 0) return NQ_EINVAL;
+  const int64_t n = (int64_t)v.size();
+  if (cap >= n && n > 0) {
+    if (!roots || !infos || !words) return NQ_EINVAL;
+    for (int64_t i = 0; i < n; i++) {
+      if (v[i].T + 1 > stride) return NQ_ESTACK;
+      for (int q = 0; q < 4; q++) roots[i * 4 + q] = v[i].root[q];
+      infos[i] = v[i].info;
+      for (int d = 0; d <= v[i].T; d++) {
+        words[(i * stride + d) * 2] = v[i].sched[2 * d];
+        words[(i * stride + d) * 2 + 1] = v[i].sched[2 * d + 1];
+      }
+    }
+  }
+  return n;
+}
+
+int nq_count_completions(nq_handle* h, int N, int k, const int* rows, const int* cols, uint64_t* count);
+
+int nq_count(nq_handle* h, int N, int preset, uint64_t* total) {
+  if (!h || !total) return NQ_EINVAL;
+  if (N < 1 || N > kMaxN) return h->fail(NQ_EINVAL, "N=%d outside 1..27", N);
+  if (N <= 5) return nq_count_completions(h, N, 0, nullptr, nullptr, total);
+  const int p = preset > 0 ? preset : preset_for(N);
+  std::vector<GenRecord> v;
+  const int s = gen_constellations(N, p, v, 0);
+  if (s == -1) return h->fail(NQ_EINVAL, "generator: bad arguments N=%d preset=%d", N, p);
+  if (s == -2) return h->fail(NQ_EPRESET, "generator: preset %d too deep for N=%d", p, N);
+  std::vector<nq_record> r(v.size());
+  for (size_t i = 0; i < v.size(); i++) r[i] = nq_record{(uint32_t)v[i].ld, (uint32_t)v[i].rd, (uint32_t)v[i].col, v[i].startijkl};
+  return nq_exec_solutions(h, N, r.data(), (int64_t)r.size(), nullptr, total);
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// batches
+// ---------------------------------------------------------------------------
+struct nq_batch {
+  nq_handle* h = nullptr;
+  std::vector<nq_job> jobs;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t done = nullptr;
+  DevBuf rec, root, info, sched, ctrl;
+  int64_t m = 0;        // tasks
+  int maxt = 1, sw = 2, grid = 0, block = 128;
+  std::vector<int64_t> job_off, job_m;     // task range per job
+  std::vector<int> job_maxt;
+  std::vector<uint64_t> fixed_total;       // jobs resolved without tasks (0 completions)
+  uint64_t* h_out = nullptr;               // pinned: totals per job + cursor/err
+  cudaGraphExec_t graph = nullptr;
+  bool submitted = false;
+  int64_t device_bytes = 0;
+};
+
+namespace {
+
+int batch_enqueue(nq_batch* b, int use_graph) {
+  nq_handle* h = b->h;
+  const int nj = (int)b->jobs.size();
+  const size_t cb = Ctrl::bytes(nj);
+  unsigned char* c = (unsigned char*)b->ctrl.p;
+  auto enqueue = [&](cudaStream_t st) -> cudaError_t {
+    cudaError_t e = cudaMemsetAsync(c, 0, cb, st);
+    if (e != cudaSuccess) return e;
+    TaskArrays ta;
+    ta.root = (uint4*)b->root.p; ta.info = (uint2*)b->info.p; ta.sched = b->sched.p; ta.sw = b->sw; ta.wide = true;
+    DfsLaunch L;
+    L.tasks = ta; L.m = b->m; L.cursor = (unsigned int*)(c + (size_t)nj * 8);
+    L.job_totals = (unsigned long long*)c; L.err = (unsigned int*)(c + (size_t)nj * 8 + 4);
+    L.maxt = b->maxt; L.block = b->block; L.grid = b->grid;
+    e = launch_dfs(L, st);
+    if (e != cudaSuccess) return e;
+    return cudaMemcpyAsync(b->h_out, c, cb, cudaMemcpyDeviceToHost, st);
+  };
+  NQ_CUDA(h, cudaSetDevice(h->device));
+  if (use_graph) {
+    if (!b->graph) {
+      cudaGraph_t g = nullptr;
+      NQ_CUDA(h, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+      cudaError_t e = enqueue(b->stream);
+      cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
+      if (e != cudaSuccess) { if (g) cudaGraphDestroy(g); return h->cuda_fail(e, "batch capture"); }
+      if (e2 != cudaSuccess) return h->cuda_fail(e2, "cudaStreamEndCapture");
+      e = cudaGraphInstantiate(&b->graph, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) { b->graph = nullptr; return h->cuda_fail(e, "cudaGraphInstantiate"); }
+    }
+    NQ_CUDA(h, cudaGraphLaunch(b->graph, b->stream));
+  } else {
+    NQ_CUDA(h, enqueue(b->stream));
+  }
+  NQ_CUDA(h, cudaEventRecord(b->done, b->stream));
+  b->submitted = true;
+  return NQ_OK;
+}
+
+int batch_collect(nq_batch* b, uint64_t* totals) {
+  nq_handle* h = b->h;
+  const int nj = (int)b->jobs.size();
+  const uint32_t e = ((const uint32_t*)(b->h_out + nj))[1];
+  b->submitted = false;
+  if (e) return h->fail(derr_to_status(e), "device: %s", derr_text(e));
+  if (totals)
+    for (int j = 0; j < nj; j++) totals[j] = b->h_out[j] + b->fixed_total[j];
+  return NQ_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void nq_batch_destroy(nq_batch* b) {
+  if (!b) return;
+  cudaSetDevice(b->h->device);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  b->rec.release(); b->root.release(); b->info.release(); b->sched.release(); b->ctrl.release();
+  if (b->h_out) cudaFreeHost(b->h_out);
+  if (b->done) cudaEventDestroy(b->done);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+}
+
+int nq_batch_create(nq_handle* h, const nq_job* jobs, int njobs, nq_batch** out) {
+  if (!h || !out || njobs <= 0 || !jobs) return h ? h->fail(NQ_EINVAL, "batch: bad arguments") : NQ_EINVAL;
+  *out = nullptr;
+  NQ_CUDA(h, cudaSetDevice(h->device));
+  nq_batch* b = new (std::nothrow) nq_batch();
+  if (!b) return NQ_ENOMEM;
+  b->h = h;
+  b->jobs.assign(jobs, jobs + njobs);
+  b->block = h->block;
+  b->job_off.assign(njobs, 0); b->job_m.assign(njobs, 0); b->job_maxt.assign(njobs, 1); b->fixed_total.assign(njobs, 0);
+  // Build: count jobs (N >= 6) become constellation records prepared on the
+  // device; count jobs with N <= 5 and completion jobs become host tasks.
+  struct Seg { int job, N; int64_t rec_off, m; };
+  std::vector<Seg> segs;
+  std::vector<nq_record> recs;
+  std::vector<HostTask> htasks;
+  std::vector<int64_t> job_host_begin(njobs, -1), job_host_end(njobs, -1);
+  int maxt = 1;
+  for (int j = 0; j < njobs; j++) {
+    const nq_job& J = jobs[j];
+    if (J.N < 1 || J.N > kMaxN || J.k < 0 || J.k > 8) { nq_batch_destroy(b); return h->fail(NQ_EINVAL, "batch job %d: bad N or k", j); }
+    if (J.kind == NQ_JOB_COUNT && J.N >= 6) {
+      const int p = J.preset > 0 ? J.preset : preset_for(J.N);
+      std::vector<GenRecord> v;
+      const int s = gen_constellations(J.N, p, v, 0);
+      if (s != 0) { nq_batch_destroy(b); return h->fail(s == -2 ? NQ_EPRESET : NQ_EINVAL, "batch job %d: generator failed", j); }
+      Seg sg{j, J.N, (int64_t)recs.size(), (int64_t)v.size()};
+      int smin = 64;
+      for (auto& g : v) {
+        recs.push_back(nq_record{(uint32_t)g.ld, (uint32_t)g.rd, (uint32_t)g.col, g.startijkl});
+        smin = std::min<int>(smin, (int)(g.startijkl >> 20));
+      }
+      segs.push_back(sg);
+      b->job_maxt[j] = maxt_for(J.N, smin);
+      maxt = std::max(maxt, b->job_maxt[j]);
+    } else if (J.kind == NQ_JOB_COUNT || J.kind == NQ_JOB_COMPLETION) {
+      int rows[8], cols[8];
+      const int k = (J.kind == NQ_JOB_COUNT) ? 0 : J.k;
+      for (int q = 0; q < k; q++) { rows[q] = J.rows[q]; cols[q] = J.cols[q]; }
+      int mt = 0;
+      const int64_t before = (int64_t)htasks.size();
+      const int s = build_completion_tasks(J.N, k, rows, cols, 4096, (uint32_t)j, htasks, &mt);
+      if (s < 0) { nq_batch_destroy(b); return h->fail(NQ_EINVAL, "batch job %d: bad pre-placed queens", j); }
+      job_host_begin[j] = before; job_host_end[j] = (int64_t)htasks.size();
+      b->job_maxt[j] = std::max(1, mt);
+      maxt = std::max(maxt, b->job_maxt[j]);
+    } else {
+      nq_batch_destroy(b);
+      return h->fail(NQ_EINVAL, "batch job %d: unknown kind %d", j, J.kind);
+    }
+  }
+  if (maxt >= kMaxDepth) { nq_batch_destroy(b); return h->fail(NQ_ESTACK, "batch: schedule too deep"); }
+  b->maxt = maxt; b->sw = maxt + 1;
+  const int64_t m_rec = (int64_t)recs.size(), m_host = (int64_t)htasks.size();
+  b->m = m_rec + m_host;
+  for (auto& sg : segs) { b->job_off[sg.job] = sg.rec_off; b->job_m[sg.job] = sg.m; }
+  for (int j = 0; j < njobs; j++)
+    if (job_host_begin[j] >= 0) { b->job_off[j] = m_rec + job_host_begin[j]; b->job_m[j] = job_host_end[j] - job_host_begin[j]; }
+  const size_t cb = Ctrl::bytes(njobs);
+  cudaError_t e;
+  if ((e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+      (e = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming)) != cudaSuccess ||
+      (e = cudaMallocHost((void**)&b->h_out, cb)) != cudaSuccess ||
+      (e = b->ctrl.ensure(cb)) != cudaSuccess ||
+      (e = b->root.ensure((size_t)std::max<int64_t>(b->m, 1) * sizeof(uint4))) != cudaSuccess ||
+      (e = b->info.ensure((size_t)std::max<int64_t>(b->m, 1) * sizeof(uint2))) != cudaSuccess ||
+      (e = b->sched.ensure((size_t)std::max<int64_t>(b->m, 1) * b->sw * sizeof(uint2))) != cudaSuccess ||
+      (e = b->rec.ensure((size_t)std::max<int64_t>(m_rec, 1) * sizeof(nq_record))) != cudaSuccess) {
+    int st = h->cuda_fail(e, "batch allocation");
+    nq_batch_destroy(b);
+    return st;
+  }
+  b->device_bytes = (int64_t)(b->root.cap + b->info.cap + b->sched.cap + b->rec.cap + b->ctrl.cap);
+  TaskArrays ta;
+  ta.root = (uint4*)b->root.p; ta.info = (uint2*)b->info.p; ta.sched = b->sched.p; ta.sw = b->sw; ta.wide = true;
+  unsigned char* c = (unsigned char*)b->ctrl.p;
+  unsigned int* derr = (unsigned int*)(c + (size_t)njobs * 8 + 4);
+  cudaStream_t st = b->stream;
+  int status = NQ_OK;
+  do {
+    if ((e = cudaMemsetAsync(c, 0, cb, st)) != cudaSuccess) break;
+    if (m_rec && (e = cudaMemcpyAsync(b->rec.p, recs.data(), (size_t)m_rec * sizeof(nq_record), cudaMemcpyHostToDevice, st)) != cudaSuccess) break;
+    for (auto& sg : segs)
+      if ((e = launch_prepare(sg.N, sg.m, (const uint4*)b->rec.p + sg.rec_off, ta, sg.rec_off, (uint32_t)sg.job, derr, st)) != cudaSuccess) break;
+    if (e != cudaSuccess) break;
+    if (m_host) {
+      std::vector<uint4> hr(m_host);
+      std::vector<uint2> hi(m_host);
+      std::vector<uint2> hs((size_t)m_host * b->sw, make_uint2(0, 0));
+      for (int64_t i = 0; i < m_host; i++) {
+        const HostTask& t = htasks[i];
+        hr[i] = make_uint4(t.root[0], t.root[1], t.root[2], t.root[3]);
+        hi[i] = make_uint2(t.info, t.job);
+        for (int d = 0; d <= t.T; d++) hs[(size_t)i * b->sw + d] = make_uint2(t.sched[2 * d], t.sched[2 * d + 1]);
+      }
+      if ((e = cudaMemcpyAsync((uint4*)b->root.p + m_rec, hr.data(), m_host * sizeof(uint4), cudaMemcpyHostToDevice, st)) != cudaSuccess) break;
+      if ((e = cudaMemcpyAsync((uint2*)b->info.p + m_rec, hi.data(), m_host * sizeof(uint2), cudaMemcpyHostToDevice, st)) != cudaSuccess) break;
+      if ((e = cudaMemcpyAsync((uint2*)b->sched.p + (size_t)m_rec * b->sw, hs.data(), hs.size() * sizeof(uint2),
+                               cudaMemcpyHostToDevice, st)) != cudaSuccess) break;
+      if ((e = cudaStreamSynchronize(st)) != cudaSuccess) break;   // host staging vectors go out of scope
+    }
+    if ((e = cudaMemcpyAsync(b->h_out, c, cb, cudaMemcpyDeviceToHost, st)) != cudaSuccess) break;
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) break;
+    const uint32_t de = ((const uint32_t*)(b->h_out + njobs))[1];
+    if (de) status = h->fail(derr_to_status(de), "batch prepare: %s", derr_text(de));
+  } while (0);
+  if (e != cudaSuccess) status = h->cuda_fail(e, "batch build");
+  if (status != NQ_OK) { nq_batch_destroy(b); return status; }
+  *out = b;
+  return NQ_OK;
+}
+
+int64_t nq_batch_tasks(const nq_batch* b) { return b ? b->m : NQ_EINVAL; }
+int64_t nq_batch_device_bytes(const nq_batch* b) { return b ? b->device_bytes : NQ_EINVAL; }
+
+int nq_batch_submit(nq_batch* b, int use_graph) {
+  if (!b) return NQ_EINVAL;
+  if (b->submitted) return b->h->fail(NQ_EBUSY, "batch already submitted");
+  return batch_enqueue(b, use_graph);
+}
+
+int nq_batch_poll(nq_batch* b, uint64_t* totals, int64_t max_wait_us) {
+  if (!b) return NQ_EINVAL;
+  if (!b->submitted) return b->h->fail(NQ_EINVAL, "batch not submitted");
+  const auto t0 = std::chrono::steady_clock::now();
+  for (;;) {
+    cudaError_t q = cudaEventQuery(b->done);
+    if (q == cudaSuccess) break;
+    if (q != cudaErrorNotReady) return b->h->cuda_fail(q, "cudaEventQuery");
+    const int64_t us = std::chrono::duration_cast<std::chrono::microseconds>(std::chrono::steady_clock::now() - t0).count();
+    if (us >= max_wait_us) return NQ_EBUSY;
+    std::this_thread::sleep_for(std::chrono::microseconds(20));
+  }
+  return batch_collect(b, totals);
+}
+
+int nq_batch_run(nq_batch* b, int use_graph, uint64_t* totals) {
+  if (!b) return NQ_EINVAL;
+  if (int s = nq_batch_submit(b, use_graph)) return s;
+  NQ_CUDA(b->h, cudaEventSynchronize(b->done));
+  return batch_collect(b, totals);
+}
+
+int nq_batch_run_plain(nq_batch* b, uint64_t* totals) {
+  if (!b) return NQ_EINVAL;
+  nq_handle* h = b->h;
+  const int nj = (int)b->jobs.size();
+  unsigned char* c = (unsigned char*)b->ctrl.p;
+  NQ_CUDA(h, cudaSetDevice(h->device));
+  for (int j = 0; j < nj; j++) {
+    uint64_t t = 0;
+    if (b->job_m[j] > 0) {
+      NQ_CUDA(h, cudaMemsetAsync(c, 0, 16, b->stream));
+      TaskArrays ta;
+      ta.root = (uint4*)b->root.p + b->job_off[j]; ta.info = (uint2*)b->info.p + b->job_off[j];
+      ta.sched = (uint2*)b->sched.p + (size_t)b->job_off[j] * b->sw; ta.sw = b->sw; ta.wide = true;
+      // One job per launch: its tasks carry job id j, which lands in slot 0.
+      DfsLaunch L;
+      L.tasks = ta; L.m = b->job_m[j]; L.cursor = (unsigned int*)(c + 8);
+      L.job_totals = (unsigned long long*)c; L.job_base = (uint32_t)j; L.err = (unsigned int*)(c + 12);
+      L.maxt = b->job_maxt[j]; L.block = b->block; L.grid = b->grid;
+      NQ_CUDA(h, launch_dfs(L, b->stream));
+      NQ_CUDA(h, cudaMemcpyAsync(b->h_out, c, 16, cudaMemcpyDeviceToHost, b->stream));
+      NQ_CUDA(h, cudaStreamSynchronize(b->stream));
+      const uint32_t e = ((const uint32_t*)b->h_out)[3];
+      if (e) return h->fail(derr_to_status(e), "device: %s", derr_text(e));
+      t = b->h_out[0];
+    }
+    if (totals) totals[j] = t + b->fixed_total[j];
+  }
+  return NQ_OK;
+}
+
+int nq_count_completions(nq_handle* h, int N, int k, const int* rows, const int* cols, uint64_t* count) {
+  if (!h || !count || k < 0 || k > 8 || (k > 0 && (!rows || !cols))) return h ? h->fail(NQ_EINVAL, "bad arguments") : NQ_EINVAL;
+  if (N < 1 || N > kMaxN) return h->fail(NQ_EINVAL, "N=%d outside 1..27", N);
+  nq_job J;
+  std::memset(&J, 0, sizeof J);
+  J.kind = NQ_JOB_COMPLETION; J.N = N; J.k = k;
+  for (int q = 0; q < k; q++) {
+    if (rows[q] < 0 || rows[q] >= N || cols[q] < 0 || cols[q] >= N) return h->fail(NQ_EINVAL, "queen outside the board");
+    J.rows[q] = (int8_t)rows[q]; J.cols[q] = (int8_t)cols[q];
+  }
+  nq_batch* b = nullptr;
+  if (int s = nq_batch_create(h, &J, 1, &b)) return s;
+  const int s = nq_batch_run(b, 0, count);
+  nq_batch_destroy(b);
+  return s;
+}
+
+}  // extern "C"

@@ -1,0 +1,56 @@
+// nq_internal.h -- internal interface between the C-ABI layer (nq_capi.cu),
+// the host task builders (nq_host.cpp) and the sm_103a kernels
+// (nq_kernels.cu).  Not installed; the public interface is
+// include/nqueens_gb300.h.
+#pragma once
+#include <stdint.h>
+#include <cuda_runtime.h>
+
+namespace nq {
+
+// Device-side error bits (OR-ed into a device word, read back by the host).
+constexpr uint32_t DERR_SHIFT = 1u;      // a record needs a negative shift (reference would raise)
+constexpr uint32_t DERR_DEPTH = 2u;      // a task's schedule is deeper than the launch's stack
+constexpr uint32_t DERR_NOTERM = 4u;     // a schedule never reaches a base frame
+constexpr uint32_t DERR_BADN = 8u;       // N outside 6..27 in a task
+
+// Prepared task arrays (structure of arrays, one entry per task).
+struct TaskArrays {
+  uint4* root = nullptr;      // {ld, rd, col, avail} of the root frame
+  uint2* info = nullptr;      // {info word (T, wexp, root count, N, status), job id}
+  void* sched = nullptr;      // per-task schedule words, stride `sw` words
+  int sw = 0;                 // schedule words per task (>= T+1 of every task)
+  bool wide = false;          // uint2 words (mixed batches) instead of uint32
+};
+
+struct DfsLaunch {
+  TaskArrays tasks;
+  int64_t m = 0;                        // number of tasks in the queue
+  const uint32_t* order = nullptr;      // optional queue order (task index per slot)
+  unsigned int* cursor = nullptr;       // queue cursor (device, zeroed before launch)
+  unsigned long long* job_totals = nullptr;  // weighted totals, slot (job id - job_base) (device)
+  uint32_t job_base = 0;
+  unsigned long long* per_task = nullptr;    // optional weighted count per task (device)
+  unsigned int* err = nullptr;          // device error word
+  int maxt = 0;                         // stack frames per lane (>= T of every task)
+  int block = 128;
+  int grid = 0;                         // 0: one wave of resident blocks
+};
+
+// Prepare: records {ld, rd, col, startijkl} (the reference's 16-byte task
+// record) -> task arrays.  job/offset place the tasks of one job inside a
+// larger queue.
+cudaError_t launch_prepare(int N, int64_t m, const uint4* records, const TaskArrays& out, int64_t offset,
+                           uint32_t job, unsigned int* err, cudaStream_t st);
+
+cudaError_t launch_dfs(const DfsLaunch& L, cudaStream_t st);
+
+// Largest block count per SM for a given stack depth (occupancy query).
+int dfs_blocks_per_sm(bool wide, int block, int maxt);
+
+// INT32 throughput probe: grid x 256 threads x iters x 128 instructions of
+// one kind (0 lop3, 1 add, 2 shf, 3 mix).
+cudaError_t int_peak(int kind, int iters, int grid, uint32_t* out, cudaStream_t st);
+size_t dfs_smem_bytes(bool wide, int block, int maxt);
+
+}  // namespace nq

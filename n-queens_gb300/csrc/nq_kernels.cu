@@ -1,0 +1,324 @@
+// nq_kernels.cu -- sm_103a kernels of the constellation DFS.
+//
+// prepare_kernel: one thread per constellation record.  It runs the task
+//   decision tree of build_soa_for_range (356Py_savesp_narrow.py:1971-2169)
+//   and walks the SQ* state machine once (356Py:689-756 does this per thread
+//   inside the reference kernel) to write the task's root frame, info word
+//   and per-depth schedule.
+//
+// dfs_kernel: persistent, explicit-stack bitboard DFS replacing
+//   kernel_dfs_iter_gpu_maxd14..21 (356Py:618-1747) and dfs_iter
+//   (356Py:1837-1967).  Every lane runs its own task; a lane whose task is
+//   done takes the next one from a global queue (one atomicAdd per warp and
+//   refill round, ranks by ballot).  Each loop iteration every busy lane
+//   expands exactly one candidate queen, so lanes stay converged on the same
+//   short instruction sequence whatever their task, depth or SQ* variant:
+//   the variant lives in the schedule word read from shared memory, not in
+//   control flow.  The current frame is in registers; saved frames (only
+//   those with candidates left, as the reference's packed stack) sit in
+//   shared memory, interleaved by lane so every access is conflict-free.
+//   Counts are summed per lane in u64 and flushed per job with one atomicAdd
+//   per warp (shuffle tree) at exit or per task when the job id changes.
+#include "nq_common.cuh"
+#include "nq_internal.h"
+
+namespace nq {
+
+constexpr unsigned FULL = 0xFFFFFFFFu;
+
+template <bool WIDE> struct WordT { using type = uint32_t; };
+template <> struct WordT<true> { using type = uint2; };
+
+// ---------------------------------------------------------------------------
+// prepare
+// ---------------------------------------------------------------------------
+template <bool WIDE>
+__global__ void __launch_bounds__(256) prepare_kernel(int N, int64_t m, const uint4* __restrict__ rec,
+                                                      uint4* __restrict__ root, uint2* __restrict__ info,
+                                                      typename WordT<WIDE>::type* __restrict__ sched, int sw,
+                                                      int64_t offset, uint32_t job, unsigned int* err) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  const uint4 r = rec[i];
+  const int64_t t = offset + i;
+  uint32_t status = TS_OK;
+  Root rt = {0, 0, 0, 0};
+  uint32_t root_count = 0;
+  int T = -1;
+  int wexp = 0;
+  Op ops[kMaxDepth];
+  if (N < 6 || N > kMaxN) {
+    status = TS_BADN;
+  } else {
+    const TaskHead h = decode_record(N, r.x, r.y, r.z, r.w);
+    wexp = h.wexp;
+    status = h.status;
+    if (status == TS_OK) {
+      const int lim = sw < kMaxDepth ? sw : kMaxDepth;
+      T = walk_schedule(N, h, &rt, &root_count, ops, lim);
+      if (T == -2) status = (lim < kMaxDepth) ? TS_DEPTH : TS_NOTERM;
+    }
+  }
+  if (status != TS_OK) {
+    atomicOr(err, status == TS_BAD_SHIFT ? DERR_SHIFT : status == TS_DEPTH ? DERR_DEPTH
+                : status == TS_NOTERM ? DERR_NOTERM : DERR_BADN);
+    T = -1; rt = {0, 0, 0, 0}; root_count = 0;
+  }
+  const uint32_t Tw = (T < 0) ? INFO_NO_DFS : (uint32_t)T;
+  root[t] = make_uint4(rt.ld, rt.rd, rt.col, T < 0 ? 0u : rt.avail);
+  info[t] = make_uint2(info_pack(Tw, (uint32_t)wexp, root_count, (uint32_t)N, status), job);
+  if (T >= 0) {
+    typename WordT<WIDE>::type* s = sched + t * sw;
+    for (int d = 0; d <= T; d++) {
+      if constexpr (WIDE) s[d] = make_uint2(pack_wide_x(ops[d]), ops[d].ra);
+      else s[d] = pack_compact(ops[d]);
+    }
+  }
+}
+
+cudaError_t launch_prepare(int N, int64_t m, const uint4* records, const TaskArrays& out, int64_t offset,
+                           uint32_t job, unsigned int* err, cudaStream_t st) {
+  if (m <= 0) return cudaSuccess;
+  const int B = 256;
+  const unsigned G = (unsigned)((m + B - 1) / B);
+  if (out.wide)
+    prepare_kernel<true><<<G, B, 0, st>>>(N, m, records, out.root, out.info, (uint2*)out.sched, out.sw, offset, job, err);
+  else
+    prepare_kernel<false><<<G, B, 0, st>>>(N, m, records, out.root, out.info, (uint32_t*)out.sched, out.sw, offset, job,
+                                           err);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// DFS
+// ---------------------------------------------------------------------------
+struct DfsArgs {
+  const uint4* root;
+  const uint2* info;
+  const void* sched;
+  int sw;
+  int64_t m;
+  const uint32_t* order;
+  unsigned int* cursor;
+  unsigned long long* job_totals;
+  uint32_t job_base;
+  unsigned long long* per_task;
+  unsigned int* err;
+  int maxt;
+};
+
+__device__ __forceinline__ void flush_job(const DfsArgs& a, unsigned job, unsigned long long v) {
+  if (v) atomicAdd(a.job_totals + (job - a.job_base), v);
+}
+
+template <bool WIDE, int BLOCK>
+__global__ void __launch_bounds__(BLOCK) dfs_kernel(const DfsArgs a) {
+  using W = typename WordT<WIDE>::type;
+  extern __shared__ __align__(16) unsigned char smem[];
+  uint4* stk = reinterpret_cast<uint4*>(smem) + threadIdx.x;                             // stride BLOCK
+  W* sch = reinterpret_cast<W*>(smem + (size_t)a.maxt * BLOCK * sizeof(uint4)) + threadIdx.x;  // stride BLOCK
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  const W* __restrict__ gsched = reinterpret_cast<const W*>(a.sched);
+
+  uint32_t ld = 0, rd = 0, col = 0, avail = 0, bm = 0;
+  uint32_t d = 0, sp = 0;
+  unsigned long long cnt = 0;   // unweighted count of the current task
+  uint32_t wexp = 0, job = a.job_base;
+  int64_t task = -1;
+  bool have = false, exhausted = false;
+  unsigned long long acc = 0;   // weighted count not yet flushed
+  uint32_t acc_job = a.job_base;
+
+  for (;;) {
+    const bool idle = (avail == 0) && (sp == 0);
+    if (idle && have) {
+      const unsigned long long v = cnt << wexp;
+      if (a.per_task) a.per_task[task] = v;
+      if (job != acc_job) { flush_job(a, acc_job, acc); acc = 0; acc_job = job; }
+      acc += v;
+      have = false;
+    }
+    const bool want = idle && !exhausted;
+    const unsigned need = __ballot_sync(FULL, want);
+    if (need) {
+      const int leader = __ffs(need) - 1;
+      unsigned base = 0;
+      if ((int)lane == leader) base = atomicAdd(a.cursor, (unsigned)__popc(need));
+      base = __shfl_sync(FULL, base, leader);
+      if (want) {
+        const uint64_t slot = (uint64_t)base + (uint64_t)__popc(need & lt_mask);
+        if (slot < (uint64_t)a.m) {
+          const uint32_t t = a.order ? a.order[slot] : (uint32_t)slot;
+          const uint4 r = a.root[t];
+          const uint2 in = a.info[t];
+          const uint32_t T = info_T(in.x);
+          task = t; have = true;
+          cnt = info_root(in.x);
+          wexp = info_wexp(in.x);
+          job = in.y;
+          bm = (1u << info_N(in.x)) - 1u;
+          d = 0; sp = 0;
+          if (T == INFO_NO_DFS || info_status(in.x) != TS_OK) {
+            avail = 0;
+          } else if ((int)T >= a.maxt) {
+            atomicOr(a.err, DERR_DEPTH);
+            avail = 0;
+          } else {
+            ld = r.x; rd = r.y; col = r.z; avail = r.w;
+            const W* src = gsched + (size_t)t * a.sw;
+            for (uint32_t k = 0; k <= T; k++) sch[k * BLOCK] = src[k];
+          }
+        } else {
+          exhausted = true;
+        }
+      }
+    }
+    if (__all_sync(FULL, exhausted && avail == 0 && sp == 0)) break;
+
+    if (avail == 0 && sp != 0) {          // resume the nearest saved frame
+      --sp;
+      const uint4 f = stk[sp * BLOCK];
+      ld = f.x; rd = f.y; col = f.z;
+      avail = f.w & 0x07FFFFFFu;
+      d = f.w >> 27;
+    }
+    if (avail != 0) {                     // expand one candidate queen
+      const uint32_t bit = avail & (0u - avail);
+      avail ^= bit;
+      const W w = sch[d * BLOCK];
+      uint32_t s, la, ra, fc, term, b14, tall;
+      if constexpr (WIDE) {
+        s = (w.x >> W_SSHIFT) & 7u; la = w.x & W_LA; ra = w.y;
+        fc = w.x & W_FC; term = w.x & W_TERM; b14 = w.x & W_B14; tall = w.x & W_TALL;
+      } else {
+        s = w >> C_SSHIFT; la = w & C_LA; ra = w & C_RA;
+        fc = w & C_FC; term = w & C_TERM; b14 = w & C_B14; tall = w & C_TALL;
+      }
+      const uint32_t nld = ((ld | bit) << s) | la;
+      const uint32_t nrd = ((rd | bit) >> s) | ra;
+      const uint32_t ncol = col | bit;
+      uint32_t nf = bm & ~(nld | nrd | ncol);
+      if (fc && (bm & ~((nld << 1) | (nrd >> 1) | ncol)) == 0u) nf = 0;
+      if (term) {
+        const uint32_t tm = b14 ? ~1u : ~0u;
+        cnt += ((nf & tm) != 0u || tall) ? 1ull : 0ull;
+      } else if (nf != 0u) {
+        if (avail != 0u) { stk[sp * BLOCK] = make_uint4(ld, rd, col, avail | (d << 27)); ++sp; }
+        ld = nld; rd = nrd; col = ncol; avail = nf; ++d;
+      }
+    }
+  }
+
+  // Flush: one atomic per warp when the warp's lanes share a job, else per lane.
+  const uint32_t j0 = __shfl_sync(FULL, acc_job, 0);
+  const bool same = __all_sync(FULL, acc == 0 || acc_job == j0);
+  if (same) {
+    unsigned long long v = acc;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+    if (lane == 0) flush_job(a, j0, v);
+  } else {
+    flush_job(a, acc_job, acc);
+  }
+}
+
+size_t dfs_smem_bytes(bool wide, int block, int maxt) {
+  return (size_t)block * ((size_t)maxt * sizeof(uint4) + (size_t)(maxt + 1) * (wide ? 8 : 4));
+}
+
+template <bool WIDE, int BLOCK>
+static cudaError_t launch_dfs_t(const DfsLaunch& L, cudaStream_t st) {
+  const size_t smem = dfs_smem_bytes(WIDE, BLOCK, L.maxt);
+  cudaError_t e = cudaFuncSetAttribute(dfs_kernel<WIDE, BLOCK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  int grid = L.grid;
+  if (grid <= 0) {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, dfs_kernel<WIDE, BLOCK>, BLOCK, smem);
+    if (e != cudaSuccess) return e;
+    if (per <= 0) return cudaErrorInvalidConfiguration;
+    grid = sms * per;
+  }
+  DfsArgs a;
+  a.root = L.tasks.root; a.info = L.tasks.info; a.sched = L.tasks.sched; a.sw = L.tasks.sw;
+  a.m = L.m; a.order = L.order; a.cursor = L.cursor; a.job_totals = L.job_totals; a.job_base = L.job_base; a.per_task = L.per_task;
+  a.err = L.err; a.maxt = L.maxt;
+  dfs_kernel<WIDE, BLOCK><<<grid, BLOCK, smem, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_dfs(const DfsLaunch& L, cudaStream_t st) {
+  if (L.m <= 0) return cudaSuccess;
+  if (L.maxt < 1 || L.maxt > kMaxDepth) return cudaErrorInvalidValue;
+  switch (L.block) {
+    case 64: return L.tasks.wide ? launch_dfs_t<true, 64>(L, st) : launch_dfs_t<false, 64>(L, st);
+    case 128: return L.tasks.wide ? launch_dfs_t<true, 128>(L, st) : launch_dfs_t<false, 128>(L, st);
+    case 256: return L.tasks.wide ? launch_dfs_t<true, 256>(L, st) : launch_dfs_t<false, 256>(L, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <bool WIDE, int BLOCK>
+static int occ(int maxt) {
+  const size_t smem = dfs_smem_bytes(WIDE, BLOCK, maxt);
+  if (cudaFuncSetAttribute(dfs_kernel<WIDE, BLOCK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return 0;
+  int per = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, dfs_kernel<WIDE, BLOCK>, BLOCK, smem) != cudaSuccess) return 0;
+  return per;
+}
+
+int dfs_blocks_per_sm(bool wide, int block, int maxt) {
+  switch (block) {
+    case 64: return wide ? occ<true, 64>(maxt) : occ<false, 64>(maxt);
+    case 128: return wide ? occ<true, 128>(maxt) : occ<false, 128>(maxt);
+    case 256: return wide ? occ<true, 256>(maxt) : occ<false, 256>(maxt);
+    default: return 0;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// INT32 ALU throughput probe: 8 independent dependency chains per thread of
+// one integer instruction kind (lop3, iadd3, shf or a 1:1:1 mix), used as the
+// measured denominator of the DFS kernel's ALU roofline.
+// ---------------------------------------------------------------------------
+template <int KIND>
+__global__ void __launch_bounds__(256) int_peak_kernel(uint32_t* out, int iters, uint32_t seed) {
+  uint32_t a[8];
+#pragma unroll
+  for (int c = 0; c < 8; c++) a[c] = seed * (c + 1) + threadIdx.x * 7919u + blockIdx.x;
+  const uint32_t b = seed ^ 0x9e3779b9u, k = (seed >> 3) | 1u;
+  for (int i = 0; i < iters; i++) {
+#pragma unroll
+    for (int u = 0; u < 16; u++) {
+#pragma unroll
+      for (int c = 0; c < 8; c++) {
+        if (KIND == 0 || (KIND == 3 && u % 3 == 0))
+          asm volatile("lop3.b32 %0, %0, %1, %2, 0x96;" : "+r"(a[c]) : "r"(b), "r"(k));
+        else if (KIND == 1 || (KIND == 3 && u % 3 == 1))
+          asm volatile("add.u32 %0, %0, %1;" : "+r"(a[c]) : "r"(b));
+        else
+          asm volatile("shf.l.wrap.b32 %0, %0, %0, %1;" : "+r"(a[c]) : "r"(k));
+      }
+    }
+  }
+  uint32_t x = 0;
+#pragma unroll
+  for (int c = 0; c < 8; c++) x ^= a[c];
+  if (x == 0x12345678u) out[0] = x;   // keeps the chains live
+}
+
+cudaError_t int_peak(int kind, int iters, int grid, uint32_t* out, cudaStream_t st) {
+  switch (kind) {
+    case 0: int_peak_kernel<0><<<grid, 256, 0, st>>>(out, iters, 12345u); break;
+    case 1: int_peak_kernel<1><<<grid, 256, 0, st>>>(out, iters, 12345u); break;
+    case 2: int_peak_kernel<2><<<grid, 256, 0, st>>>(out, iters, 12345u); break;
+    default: int_peak_kernel<3><<<grid, 256, 0, st>>>(out, iters, 12345u); break;
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace nq

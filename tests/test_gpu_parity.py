@@ -1,0 +1,205 @@
+"""GPU parity: the sm_103a kernels through the C ABI against the oracle and the
+reference's golden vectors.  Bit-exact for every count."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import REPO, gpu_available
+from golden_util import canonical_order, solution_digest
+
+pytestmark = [pytest.mark.gpu, pytest.mark.skipif(not gpu_available(), reason="needs a CUDA GPU")]
+GOLDEN = os.path.join(REPO, "tests", "golden")
+
+
+@pytest.fixture(scope="module")
+def eng():
+    import nqueens
+    e = nqueens.Engine(0)
+    yield e
+    e.close()
+
+
+def _o_records(oracle_mod, recs):
+    return oracle_mod.Records(recs["ld"].astype(np.uint64), recs["rd"].astype(np.uint64),
+                              recs["col"].astype(np.uint64), recs["startijkl"].copy())
+
+
+@pytest.mark.parametrize("N", range(6, 20))
+def test_per_record_counts_match_archived_solutions(eng, N):
+    """Every record's weighted count equals the reference's archived solutions_N{N}_5_v2.bin."""
+    import nqueens
+    d = json.load(open(os.path.join(GOLDEN, "archive_digests.json")))["solutions"][str(N)]
+    ld, rd, col, s = nqueens.gen_records_wide(N, 5)
+    recs = np.zeros(len(s), nqueens.RECORD_DTYPE)
+    recs["ld"] = ld & 0xFFFFFFFF; recs["rd"] = rd & 0xFFFFFFFF; recs["col"] = col & 0xFFFFFFFF; recs["startijkl"] = s
+    total, sol = eng.exec_records(N, recs, want_solutions=True)
+    assert total == d["sum"]
+    assert solution_digest(s, ld, rd, col, sol) == d["sha256"]
+
+
+@pytest.mark.parametrize("N", range(6, 17))
+def test_per_record_counts_match_oracle_dynamic_preset(eng, oracle_mod, N):
+    import nqueens
+    recs = nqueens.gen_records(N)
+    total, sol = eng.exec_records(N, recs, want_solutions=True)
+    want = oracle_mod.exec_solutions(N, _o_records(oracle_mod, recs))
+    assert np.array_equal(sol, want)
+    assert total == oracle_mod.EXPECTED_TOTAL[N]
+
+
+@pytest.mark.parametrize("N,preset", [(10, 4), (11, 6), (12, 7), (13, 4), (14, 6), (9, 7), (8, 6)])
+def test_other_presets_match_oracle(eng, oracle_mod, N, preset):
+    import nqueens
+    recs = nqueens.gen_records(N, preset)
+    total, sol = eng.exec_records(N, recs, want_solutions=True)
+    want = oracle_mod.exec_solutions(N, _o_records(oracle_mod, recs))
+    assert np.array_equal(sol, want)
+
+
+@pytest.mark.parametrize("N", list(range(1, 20)))
+def test_totals_known_answers(eng, oracle_mod, N):
+    assert eng.count(N).total == oracle_mod.EXPECTED_TOTAL[N]
+
+
+def test_total_n20(eng, oracle_mod):
+    assert eng.count(20).total == oracle_mod.EXPECTED_TOTAL[20] == 39029188884
+
+
+def test_reference_dict_dropin(eng, oracle_mod):
+    import nqueens
+    _, _, cs, _ = nqueens.gen_constellations(11, set(), set(), [], 5)
+    nqueens.exec_solutions(11, cs, True)
+    assert sum(c["solutions"] for c in cs if c["solutions"] > 0) == 2680
+    s = np.load(os.path.join(GOLDEN, "archive_small.npz"))["N11"]
+    got = {(c["startijkl"], c["ld"], c["rd"], c["col"]): c["solutions"] for c in cs}
+    for row in s.tolist():
+        assert got[tuple(row[:4])] == row[4]
+
+
+def test_device_resident_path(eng, oracle_mod):
+    torch = pytest.importorskip("torch")
+    import nqueens
+    N = 15
+    recs = nqueens.gen_records(N)
+    d_rec = torch.from_numpy(recs.view(np.uint8).copy()).cuda()
+    d_total = torch.zeros(1, dtype=torch.int64, device="cuda")
+    d_sol = torch.zeros(len(recs), dtype=torch.int64, device="cuda")
+    start_min = int((recs["startijkl"] >> 20).min())
+    s = torch.cuda.Stream()
+    for _ in range(2):
+        eng.exec_device(N, d_rec.data_ptr(), len(recs), start_min, d_total.data_ptr(), d_sol.data_ptr(), s.cuda_stream)
+        eng.sync()
+        assert int(d_total.item()) == oracle_mod.EXPECTED_TOTAL[N]
+    want = oracle_mod.exec_solutions(N, _o_records(oracle_mod, recs))
+    assert np.array_equal(d_sol.cpu().numpy().view(np.uint64), want)
+    p, k = eng.last_kernel_ms()
+    assert p >= 0 and k > 0
+
+
+def test_preset_too_deep_is_an_error(eng):
+    import nqueens
+    recs = nqueens.gen_records(6, 6)   # the reference raises on a negative shift for this preset
+    with pytest.raises(nqueens.NQError) as ei:
+        eng.exec_records(6, recs)
+    assert ei.value.status == -6
+
+
+def test_empty_and_single_record(eng, oracle_mod):
+    import nqueens
+    assert eng.exec_records(12, np.zeros(0, nqueens.RECORD_DTYPE))[0] == 0
+    recs = nqueens.gen_records(12)
+    want = oracle_mod.exec_solutions(12, _o_records(oracle_mod, recs))
+    for i in (0, 7, len(recs) - 1):
+        t, sol = eng.exec_records(12, recs[i:i + 1], want_solutions=True)
+        assert t == int(want[i]) and int(sol[0]) == int(want[i])
+
+
+def test_ragged_and_duplicated_records(eng, oracle_mod):
+    """Records in any order, with duplicates: counts are per record."""
+    import nqueens
+    recs = nqueens.gen_records(13)
+    rng = np.random.default_rng(7)
+    idx = rng.integers(0, len(recs), size=5001)
+    sub = recs[idx]
+    t, sol = eng.exec_records(13, sub, want_solutions=True)
+    want = oracle_mod.exec_solutions(13, _o_records(oracle_mod, sub))
+    assert np.array_equal(sol, want) and t == int(want.sum())
+
+
+@pytest.mark.parametrize("block", [64, 128, 256])
+def test_launch_configs_agree(eng, oracle_mod, block):
+    import nqueens
+    eng.set_config(block, 0, 0)
+    try:
+        assert eng.count(16).total == oracle_mod.EXPECTED_TOTAL[16]
+        eng.set_config(block, 37, 0)   # a grid that is not a multiple of anything
+        assert eng.count(14).total == oracle_mod.EXPECTED_TOTAL[14]
+    finally:
+        eng.set_config(128, 0, 0)
+
+
+def _queens(rng, N, k):
+    while True:
+        rows = rng.choice(N, size=k, replace=False)
+        cols = rng.integers(0, N, size=k)
+        q = list(zip(rows.tolist(), cols.tolist()))
+        if all(q[a][1] != q[b][1] and abs(q[a][0] - q[b][0]) != abs(q[a][1] - q[b][1])
+               for a in range(k) for b in range(a + 1, k)):
+            return q
+
+
+@pytest.mark.parametrize("N", range(4, 14))
+def test_completions_match_bruteforce(eng, oracle_mod, N):
+    rng = np.random.default_rng(50 + N)
+    for k in (0, 1, 2, 3, 4):
+        q = _queens(rng, N, k)
+        want = oracle_mod.completions(N, [r for r, _ in q], [c for _, c in q])
+        assert eng.count_completions(N, q) == want, (N, q)
+
+
+def test_completion_edge_cases(eng, oracle_mod):
+    assert eng.count_completions(8, [(0, 0), (1, 1)]) == 0          # attacking
+    assert eng.count_completions(8, [(3, 3), (3, 5)]) == 0          # two queens in one row
+    import nqueens
+    with pytest.raises(nqueens.NQError):
+        eng.count_completions(8, [(3, 3), (3, 3)])                  # the same queen twice is a bad argument
+    with pytest.raises(nqueens.NQError):
+        eng.count_completions(8, [(8, 0)])                          # off the board
+    assert eng.count_completions(1, []) == 1
+    assert eng.count_completions(3, []) == 0
+    assert eng.count_completions(10, [(9, 0), (8, 2), (7, 4)]) == oracle_mod.completions(10, [9, 8, 7], [0, 2, 4])
+    assert eng.count_completions(10, [(0, 9), (1, 7), (2, 5), (3, 3)]) == oracle_mod.completions(
+        10, [0, 1, 2, 3], [9, 7, 5, 3])
+
+
+def test_batch_mixed_jobs(eng, oracle_mod):
+    import nqueens
+    rng = np.random.default_rng(2026)
+    jobs, want = [], []
+    for _ in range(40):
+        if rng.random() < 0.6:
+            N = int(rng.integers(4, 15))
+            jobs.append(nqueens.CountJob(N)); want.append(oracle_mod.EXPECTED_TOTAL[N])
+        else:
+            N = int(rng.integers(5, 13)); k = int(rng.integers(0, 5))
+            q = _queens(rng, N, k)
+            jobs.append(nqueens.CompletionJob(N, q))
+            want.append(oracle_mod.completions(N, [r for r, _ in q], [c for _, c in q]))
+    b = eng.batch(jobs)
+    try:
+        want = np.array(want, np.uint64)
+        assert np.array_equal(b.run(use_graph=False), want)
+        assert np.array_equal(b.run(use_graph=True), want)
+        assert np.array_equal(b.run(use_graph=True), want)     # graph replay
+        assert np.array_equal(b.run_plain(), want)
+        b.submit(True)
+        out = None
+        for _ in range(10000):
+            out = b.poll(1000)
+            if out is not None:
+                break
+        assert out is not None and np.array_equal(out, want)
+    finally:
+        b.close()
