@@ -108,9 +108,12 @@ int nq_debug_task_schedule(int N, nq_record rec, uint32_t root[4], uint32_t *inf
 /* Diagnostic: the host-built tasks of a completion query (see
  * nq_count_completions), wide format: per task root {ld, rd, col, avail},
  * info word and (T+1) word pairs {x, RA} at words + task * 2 * stride.
+ * *fixed_count (nullable) receives the part of the count settled without a
+ * task (1 when the pre-placed queens already fill the board, else 0).
  * Returns the task count (call with cap = 0 to size), or a negative status. */
 int64_t nq_debug_completion_tasks(int N, int k, const int *rows, const int *cols, int min_tasks,
-                                  uint32_t *roots, uint32_t *infos, uint32_t *words, int stride, int64_t cap);
+                                  uint32_t *roots, uint32_t *infos, uint32_t *words, int stride, int64_t cap,
+                                  uint64_t *fixed_count);
 
 /* Diagnostic: measured INT32 instruction throughput of the device (thread
  * instructions per second) for kind 0 = lop3, 1 = add, 2 = shf, 3 = a 1:1:1

@@ -357,12 +357,13 @@ int nq_debug_task_schedule(int N, nq_record rec, uint32_t root[4], uint32_t* inf
 }
 
 int64_t nq_debug_completion_tasks(int N, int k, const int* rows, const int* cols, int min_tasks, uint32_t* roots,
-                                  uint32_t* infos, uint32_t* words, int stride, int64_t cap) {
+                                  uint32_t* infos, uint32_t* words, int stride, int64_t cap, uint64_t* fixed_count) {
   if (k < 0 || k > 8 || (k > 0 && (!rows || !cols)) || stride < 1) return NQ_EINVAL;
   std::vector<HostTask> v;
   int mt = 0;
   const int s = build_completion_tasks(N, k, rows, cols, min_tasks, 0, v, &mt);
   if (s < 0) return NQ_EINVAL;
+  if (fixed_count) *fixed_count = (s == 2) ? 1 : 0;
   const int64_t n = (int64_t)v.size();
   if (cap >= n && n > 0) {
     if (!roots || !infos || !words) return NQ_EINVAL;
@@ -529,6 +530,7 @@ int nq_batch_create(nq_handle* h, const nq_job* jobs, int njobs, nq_batch** out)
       const int64_t before = (int64_t)htasks.size();
       const int s = build_completion_tasks(J.N, k, rows, cols, 4096, (uint32_t)j, htasks, &mt);
       if (s < 0) { nq_batch_destroy(b); return h->fail(NQ_EINVAL, "batch job %d: bad pre-placed queens", j); }
+      if (s == 2) b->fixed_total[j] = 1;
       job_host_begin[j] = before; job_host_end[j] = (int64_t)htasks.size();
       b->job_maxt[j] = std::max(1, mt);
       maxt = std::max(maxt, b->job_maxt[j]);

@@ -220,7 +220,7 @@ int build_completion_tasks(int N, int k, const int* rows, const int* cols, int m
   int F[32], n = 0;
   for (int r = 0; r < N; r++)
     if (fixed_col[r] < 0) F[n++] = r;
-  if (n == 0) return 1;   // k == N is rejected above; kept for completeness
+  if (n == 0) return 2;   // every row holds a pre-placed queen and none attack: exactly one placement
   const uint32_t bm = (N >= 32) ? 0xFFFFFFFFu : ((1u << N) - 1u);
   // root frame at row F[0]
   uint32_t ld = 0, rd = 0, col = 0;

@@ -30,8 +30,9 @@ int gen_constellations(int N, int preset, std::vector<GenRecord>& out, int threa
 
 // Tasks whose counts sum to the number of N-queens solutions containing the
 // k pre-placed queens (rows[q], cols[q]); no symmetry weight.  Returns 0 with
-// tasks appended, 1 when the count is 0 without any task (attacking or
-// duplicate queens), -1 on bad arguments.  *max_T is raised to the deepest
+// tasks appended, 1 when the count is 0 without any task (attacking queens or
+// two queens in one row), 2 when the count is 1 without any task (the queens
+// fill every row), -1 on bad arguments.  *max_T is raised to the deepest
 // task's terminal depth.
 int build_completion_tasks(int N, int k, const int* rows, const int* cols, int min_tasks, uint32_t job,
                            std::vector<HostTask>& out, int* max_T);

@@ -32,7 +32,7 @@ struct DfsLaunch {
   uint32_t job_base = 0;
   unsigned long long* per_task = nullptr;    // optional weighted count per task (device)
   unsigned int* err = nullptr;          // device error word
-  int maxt = 0;                         // stack frames per lane (>= T of every task)
+  int maxt = 0;                         // stack frames per lane (>= T of every task; words: maxt+1)
   int block = 128;
   int grid = 0;                         // 0: one wave of resident blocks
 };

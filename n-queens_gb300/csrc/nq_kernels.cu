@@ -161,7 +161,7 @@ __global__ void __launch_bounds__(BLOCK) dfs_kernel(const DfsArgs a) {
           d = 0; sp = 0;
           if (T == INFO_NO_DFS || info_status(in.x) != TS_OK) {
             avail = 0;
-          } else if ((int)T >= a.maxt) {
+          } else if ((int)T > a.maxt) {      // frames at depths 0..T-1, words 0..T
             atomicOr(a.err, DERR_DEPTH);
             avail = 0;
           } else {

@@ -75,7 +75,7 @@ SIGNATURES = {
     "nq_count_completions": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _ip, _ip, _u64p]),
     "nq_debug_task_schedule": (ctypes.c_int, [ctypes.c_int, nq_record, _u32p, _u32p, _u32p, ctypes.c_int]),
     "nq_debug_completion_tasks": (ctypes.c_int64, [ctypes.c_int, ctypes.c_int, _ip, _ip, ctypes.c_int, _u32p,
-                                                  _u32p, _u32p, ctypes.c_int, ctypes.c_int64]),
+                                                  _u32p, _u32p, ctypes.c_int, ctypes.c_int64, _u64p]),
     "nq_int32_peak": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
     "nq_batch_create": (ctypes.c_int, [_vp, ctypes.POINTER(nq_job), ctypes.c_int, ctypes.POINTER(_vp)]),
     "nq_batch_tasks": (ctypes.c_int64, [_vp]),

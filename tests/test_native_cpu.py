@@ -170,15 +170,16 @@ def completion_tasks(N, queens, min_tasks=64):
     rows = (ctypes.c_int * max(1, k))(*[q[0] for q in queens])
     cols = (ctypes.c_int * max(1, k))(*[q[1] for q in queens])
     L = _lib.lib()
-    n = L.nq_debug_completion_tasks(N, k, rows, cols, min_tasks, None, None, None, 32, 0)
+    fixed = np.zeros(1, np.uint64)
+    n = L.nq_debug_completion_tasks(N, k, rows, cols, min_tasks, None, None, None, 32, 0, _lib.p64(fixed))
     assert n >= 0
     roots = np.zeros(max(1, n) * 4, np.uint32)
     infos = np.zeros(max(1, n), np.uint32)
     words = np.zeros(max(1, n) * 32 * 2, np.uint32)
     n2 = L.nq_debug_completion_tasks(N, k, rows, cols, min_tasks, _lib.p32(roots), _lib.p32(infos), _lib.p32(words),
-                                     32, n)
+                                     32, n, None)
     assert n2 == n
-    out = []
+    out = [([0, 0, 0, 0], 31 | (int(fixed[0]) << 7), [])] if fixed[0] else []
     for i in range(n):
         T = int(infos[i]) & 31
         w = [(int(words[(i * 32 + d) * 2]), int(words[(i * 32 + d) * 2 + 1])) for d in range(T + 1)]
@@ -215,6 +216,13 @@ def test_completion_replay_matches_bruteforce(nq, oracle_mod, N):
 def test_completion_attacking_queens_have_no_tasks(nq):
     assert completion_tasks(8, [(0, 0), (1, 1)]) == []
     assert completion_tasks(8, [(0, 3), (5, 3)]) == []
+
+
+def test_completion_full_board(nq, oracle_mod):
+    q = [(2, 0), (0, 1), (3, 2), (1, 3)]       # a full 4-queens solution
+    t = completion_tasks(4, q)
+    assert sum(replay(root, info, w, wide=True)[0] for root, info, w in t) == 1 == oracle_mod.completions(
+        4, [r for r, _ in q], [c for _, c in q])
 
 
 def test_exec_solutions_rejects_cpu_path(nq):
