@@ -197,7 +197,7 @@ def ours_arm(args):
         dist.init_process_group("nccl")
     dev = local if ws > 1 else 0
     torch.cuda.set_device(dev)
-    eng = nqueens.Engine(dev, block=args.block)
+    eng = nqueens.Engine(dev, block=args.block, split=args.split)
     N = N_BENCH
     expected = 4968057848
     recs = nqueens.gen_records(N)
@@ -236,6 +236,7 @@ def ours_arm(args):
         eng.sync()
         dfs_ms.append(eng.last_kernel_ms()[1])
         assert int(d_total.item()) == expected
+    split_depth, queued = eng.last_run_info()
     torch.cuda.synchronize()
     clk = clocks.stop()
     step_ms = [a.elapsed_time(b) for a, b in ev]
@@ -274,7 +275,8 @@ def ours_arm(args):
         "vs_baseline": None, "dtype": "u32", "data": "synthetic",
         "config": {"workload": "plain single-N count, N=19, preset 6 (897,071 tasks, 4,968,057,848 solutions), "
                                "one prepare+DFS launch pair per step",
-                   "N": N, "preset": 6, "tasks": m, "block": args.block,
+                   "N": N, "preset": 6, "tasks": m, "block": args.block, "split_depth": split_depth,
+                   "queued_subtasks": queued,
                    "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{ws}"},
         "n19_total": expected,
         "n19_wall_s": wall_n19,
@@ -289,7 +291,7 @@ def ours_arm(args):
                      "hbm_frac": (m * 16 + m * 16 + m * 8 + m * 4 * 15) / (dfs_avg * 1e-3) / (
                          (peaks or {}).get("hbm_gbs", 6800.0) * 1e9)},
         "clocks": clk,
-        "gpu_launches": 2 * args.steps,
+        "gpu_launches": (4 if split_depth > 0 else 2) * args.steps,
     }
     if rank == 0 and not args.no_cpu:
         cb = run_cpu(N, args.cpu_seconds)
@@ -311,6 +313,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--block", type=int, default=128)
+    ap.add_argument("--split", type=int, default=-1, help="split depth (-1 automatic)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()

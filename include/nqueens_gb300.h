@@ -49,10 +49,11 @@ void nq_destroy(nq_handle *h);
 int nq_last_error(const nq_handle *h, char *buf, size_t cap);
 
 /* Launch knobs chosen by the autotuner: threads per block (64, 128 or 256),
- * grid (0 = one wave of resident blocks) and queue order (0 = record order,
- * 1 = estimated cost, largest first). */
-int nq_set_config(nq_handle *h, int block, int grid, int order_mode);
-int nq_get_config(const nq_handle *h, int *block, int *grid, int *order_mode);
+ * grid (0 = one wave of resident blocks) and split depth (-1 = automatic,
+ * 0..3 = expand every task that many levels on the device before the DFS, so
+ * the queue holds many small subtasks instead of few large ones). */
+int nq_set_config(nq_handle *h, int block, int grid, int split_depth);
+int nq_get_config(const nq_handle *h, int *block, int *grid, int *split_depth);
 
 /* select_dynamic_preset_queens (356Py_savesp_narrow.py:5744-5753). */
 int nq_preset_for(int N);
@@ -75,17 +76,21 @@ int64_t nq_gen_constellations_wide(int N, int preset, uint64_t *ld, uint64_t *rd
 int nq_exec_solutions(nq_handle *h, int N, const nq_record *records, int64_t m, uint64_t *solutions,
                       uint64_t *total);
 
-/* Same on device-resident buffers, asynchronous on `stream` (NULL: the
- * handle's stream).  `start_min` is the smallest start row
- * (startijkl >> 20) over the records, or -1 to use the bound 1.
- * d_total (device, 1 x u64) is overwritten.  Call nq_sync() to wait and
- * collect the status. */
+/* Same on device-resident buffers on `stream` (NULL: the handle's stream).
+ * `start_min` is the smallest start row (startijkl >> 20) over the records,
+ * or -1 to use the bound 1.  d_total (device, 1 x u64) is overwritten.  When
+ * the queue is split the call waits once for an 8-byte subtask count before
+ * launching the DFS; otherwise it returns after enqueueing.  Call nq_sync()
+ * to wait for the result and collect the status. */
 int nq_exec_solutions_device(nq_handle *h, int N, const nq_record *d_records, int64_t m, int start_min,
                              uint64_t *d_solutions, uint64_t *d_total, void *stream);
 int nq_sync(nq_handle *h);
 /* Device time of the last exec_solutions call's prepare and DFS kernels
  * (CUDA events recorded on the launching stream); waits for them. */
 int nq_last_kernel_ms(nq_handle *h, float *prepare_ms, float *dfs_ms);
+/* Split depth used by the last exec_solutions call and the length of the
+ * DFS queue it built (records, or subtasks when split). */
+int nq_last_run_info(const nq_handle *h, int *split_depth, int64_t *queued);
 
 /* Whole-board total for N, the loop body of the reference's main()
  * (356Py_savesp_narrow.py:6036-6046): brute force on the GPU for N <= 5

@@ -67,6 +67,15 @@ const char* derr_text(uint32_t e) {
   return "ok";
 }
 
+// Expand tasks until the queue holds about 24 subtasks per resident lane
+// (each level multiplies the task count by roughly 4), at most 3 levels.
+int choose_split(int64_t m, int64_t lanes) {
+  int D = 0;
+  double est = (double)m;
+  while (D < 3 && est < 24.0 * (double)lanes) { est *= 4.0; D++; }
+  return D;
+}
+
 int maxt_for(int N, int start_min) {
   // Terminal-parent depth T <= N - 3 - start; one frame of margin.
   int s = start_min < 0 ? 1 : start_min;
@@ -80,12 +89,14 @@ struct nq_handle {
   int device = 0;
   int sms = 0;
   cudaStream_t stream = nullptr;
-  int block = 128, grid = 0, order_mode = 0;
+  int block = 128, grid = 0, split = -1;   // split: -1 automatic, 0..3 fixed depth
   std::string err;
-  DevBuf rec, root, info, sched, per_task, ctrl;
+  DevBuf rec, root, info, sched, per_task, ctrl, nsub, sroot, sinfo;
   uint64_t* h_ctrl = nullptr;   // pinned read-back of the control block
   size_t h_ctrl_cap = 0;
   bool pending = false;
+  int last_split = 0;        // split depth and queue length of the last run
+  int64_t last_queue = 0;
   // events around the last run's kernels (same stream as the launches)
   cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
 
@@ -117,7 +128,15 @@ struct nq_handle {
 
 namespace {
 
-// records (device) -> counts.  Asynchronous on st; totals land in ctrl[0].
+int64_t resident_lanes(nq_handle* h, bool wide, int maxt) {
+  const int per = dfs_blocks_per_sm(wide, h->block, maxt);
+  const int64_t grid = h->grid > 0 ? h->grid : (int64_t)h->sms * std::max(1, per);
+  return grid * h->block;
+}
+
+// records (device) -> counts on st; totals land in ctrl[0].  Launches
+// prepare, then (when splitting) the split count pass, one 8-byte read-back
+// to size the subtask queue, the split write pass, and the DFS.
 int run_records(nq_handle* h, int N, const uint4* d_rec, int64_t m, int start_min, unsigned long long* d_per_task,
                 cudaStream_t st) {
   const int maxt = maxt_for(N, start_min);
@@ -126,19 +145,37 @@ int run_records(nq_handle* h, int N, const uint4* d_rec, int64_t m, int start_mi
   NQ_CUDA(h, h->root.ensure((size_t)m * sizeof(uint4)));
   NQ_CUDA(h, h->info.ensure((size_t)m * sizeof(uint2)));
   NQ_CUDA(h, h->sched.ensure((size_t)m * sw * sizeof(uint32_t)));
-  NQ_CUDA(h, h->ctrl.ensure(Ctrl::bytes(1)));
+  NQ_CUDA(h, h->ctrl.ensure(Ctrl::bytes(1) + 16));
   unsigned char* c = (unsigned char*)h->ctrl.p;
-  NQ_CUDA(h, cudaMemsetAsync(c, 0, Ctrl::bytes(1), st));
+  NQ_CUDA(h, cudaMemsetAsync(c, 0, Ctrl::bytes(1) + 16, st));
   TaskArrays ta;
   ta.root = (uint4*)h->root.p; ta.info = (uint2*)h->info.p; ta.sched = h->sched.p; ta.sw = sw; ta.wide = false;
+  unsigned long long* totals = (unsigned long long*)c;
   unsigned int* cursor = (unsigned int*)(c + 8);
   unsigned int* err = (unsigned int*)(c + 12);
+  unsigned long long* sctr = (unsigned long long*)(c + 16);   // split: [0] subtasks, [1] allocation cursor
   NQ_CUDA(h, cudaEventRecord(h->ev[0], st));
   NQ_CUDA(h, launch_prepare(N, m, d_rec, ta, 0, 0, err, st));
-  NQ_CUDA(h, cudaEventRecord(h->ev[1], st));
+  const int D = h->split >= 0 ? h->split : choose_split(m, resident_lanes(h, false, maxt));
   DfsLaunch L;
-  L.tasks = ta; L.m = m; L.order = nullptr; L.cursor = cursor; L.job_totals = (unsigned long long*)c;
+  L.tasks = ta; L.m = m; L.order = nullptr; L.cursor = cursor; L.job_totals = totals;
   L.per_task = d_per_task; L.err = err; L.maxt = maxt; L.block = h->block; L.grid = h->grid;
+  if (D > 0) {
+    NQ_CUDA(h, h->nsub.ensure((size_t)m * sizeof(uint32_t)));
+    NQ_CUDA(h, launch_split(0, D, 0, m, ta, (uint32_t*)h->nsub.p, nullptr, nullptr, sctr, nullptr, totals, 0, st));
+    if (int s = h->ensure_pinned(Ctrl::bytes(1) + 16)) return s;
+    NQ_CUDA(h, cudaMemcpyAsync(h->h_ctrl, c, Ctrl::bytes(1) + 16, cudaMemcpyDeviceToHost, st));
+    NQ_CUDA(h, cudaStreamSynchronize(st));
+    const int64_t ns = (int64_t)h->h_ctrl[2];
+    if (ns > (int64_t)0xFFFFFFFF) return h->fail(NQ_ENOMEM, "split: %lld subtasks", (long long)ns);
+    NQ_CUDA(h, h->sroot.ensure((size_t)std::max<int64_t>(ns, 1) * sizeof(uint4)));
+    NQ_CUDA(h, h->sinfo.ensure((size_t)std::max<int64_t>(ns, 1) * sizeof(uint2)));
+    NQ_CUDA(h, launch_split(1, D, 0, m, ta, (uint32_t*)h->nsub.p, (uint4*)h->sroot.p, (uint2*)h->sinfo.p, sctr,
+                            d_per_task, totals, 0, st));
+    L.sroot = (const uint4*)h->sroot.p; L.sinfo = (const uint2*)h->sinfo.p; L.m = ns;
+  }
+  h->last_split = D; h->last_queue = L.m;
+  NQ_CUDA(h, cudaEventRecord(h->ev[1], st));
   NQ_CUDA(h, launch_dfs(L, st));
   NQ_CUDA(h, cudaEventRecord(h->ev[2], st));
   return NQ_OK;
@@ -199,6 +236,7 @@ void nq_destroy(nq_handle* h) {
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
   h->rec.release(); h->root.release(); h->info.release(); h->sched.release(); h->per_task.release(); h->ctrl.release();
+  h->nsub.release(); h->sroot.release(); h->sinfo.release();
   if (h->h_ctrl) cudaFreeHost(h->h_ctrl);
   for (auto& e : h->ev) if (e) cudaEventDestroy(e);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -230,6 +268,13 @@ int nq_int32_peak(nq_handle* h, int kind, double* ops_per_s) {
   return NQ_OK;
 }
 
+int nq_last_run_info(const nq_handle* h, int* split_depth, int64_t* queued) {
+  if (!h) return NQ_EINVAL;
+  if (split_depth) *split_depth = h->last_split;
+  if (queued) *queued = h->last_queue;
+  return NQ_OK;
+}
+
 int nq_last_kernel_ms(nq_handle* h, float* prepare_ms, float* dfs_ms) {
   if (!h) return NQ_EINVAL;
   NQ_CUDA(h, cudaSetDevice(h->device));
@@ -248,19 +293,19 @@ int nq_last_error(const nq_handle* h, char* buf, size_t cap) {
   return NQ_OK;
 }
 
-int nq_set_config(nq_handle* h, int block, int grid, int order_mode) {
+int nq_set_config(nq_handle* h, int block, int grid, int split_depth) {
   if (!h) return NQ_EINVAL;
   if (block != 64 && block != 128 && block != 256) return h->fail(NQ_EINVAL, "block must be 64, 128 or 256");
-  if (grid < 0 || order_mode < 0 || order_mode > 1) return h->fail(NQ_EINVAL, "bad grid or order mode");
-  h->block = block; h->grid = grid; h->order_mode = order_mode;
+  if (grid < 0 || split_depth < -1 || split_depth > 3) return h->fail(NQ_EINVAL, "bad grid or split depth");
+  h->block = block; h->grid = grid; h->split = split_depth;
   return NQ_OK;
 }
 
-int nq_get_config(const nq_handle* h, int* block, int* grid, int* order_mode) {
+int nq_get_config(const nq_handle* h, int* block, int* grid, int* split_depth) {
   if (!h) return NQ_EINVAL;
   if (block) *block = h->block;
   if (grid) *grid = h->grid;
-  if (order_mode) *order_mode = h->order_mode;
+  if (split_depth) *split_depth = h->split;
   return NQ_OK;
 }
 
@@ -406,12 +451,14 @@ struct nq_batch {
   std::vector<nq_job> jobs;
   cudaStream_t stream = nullptr;
   cudaEvent_t done = nullptr;
-  DevBuf rec, root, info, sched, ctrl;
+  DevBuf rec, root, info, sched, ctrl, nsub, sroot, sinfo;
   int64_t m = 0;        // tasks
+  int64_t ms = 0;       // queued subtasks (every job's split output, job after job)
   int maxt = 1, sw = 2, grid = 0, block = 128;
   std::vector<int64_t> job_off, job_m;     // task range per job
-  std::vector<int> job_maxt;
-  std::vector<uint64_t> fixed_total;       // jobs resolved without tasks (0 completions)
+  std::vector<int64_t> sub_off, sub_m;     // subtask range per job
+  std::vector<int> job_maxt, job_split;
+  std::vector<uint64_t> fixed_total;       // counts settled at build time (small tasks, full boards)
   uint64_t* h_out = nullptr;               // pinned: totals per job + cursor/err
   cudaGraphExec_t graph = nullptr;
   bool submitted = false;
@@ -431,7 +478,8 @@ int batch_enqueue(nq_batch* b, int use_graph) {
     TaskArrays ta;
     ta.root = (uint4*)b->root.p; ta.info = (uint2*)b->info.p; ta.sched = b->sched.p; ta.sw = b->sw; ta.wide = true;
     DfsLaunch L;
-    L.tasks = ta; L.m = b->m; L.cursor = (unsigned int*)(c + (size_t)nj * 8);
+    L.tasks = ta; L.sroot = (const uint4*)b->sroot.p; L.sinfo = (const uint2*)b->sinfo.p;
+    L.m = b->ms; L.cursor = (unsigned int*)(c + (size_t)nj * 8);
     L.job_totals = (unsigned long long*)c; L.err = (unsigned int*)(c + (size_t)nj * 8 + 4);
     L.maxt = b->maxt; L.block = b->block; L.grid = b->grid;
     e = launch_dfs(L, st);
@@ -481,6 +529,7 @@ void nq_batch_destroy(nq_batch* b) {
   if (b->stream) cudaStreamSynchronize(b->stream);
   if (b->graph) cudaGraphExecDestroy(b->graph);
   b->rec.release(); b->root.release(); b->info.release(); b->sched.release(); b->ctrl.release();
+  b->nsub.release(); b->sroot.release(); b->sinfo.release();
   if (b->h_out) cudaFreeHost(b->h_out);
   if (b->done) cudaEventDestroy(b->done);
   if (b->stream) cudaStreamDestroy(b->stream);
@@ -592,7 +641,43 @@ int nq_batch_create(nq_handle* h, const nq_job* jobs, int njobs, nq_batch** out)
     if ((e = cudaMemcpyAsync(b->h_out, c, cb, cudaMemcpyDeviceToHost, st)) != cudaSuccess) break;
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) break;
     const uint32_t de = ((const uint32_t*)(b->h_out + njobs))[1];
-    if (de) status = h->fail(derr_to_status(de), "batch prepare: %s", derr_text(de));
+    if (de) { status = h->fail(derr_to_status(de), "batch prepare: %s", derr_text(de)); break; }
+    // Split each job on its own (tiny boards are not split), so every job's
+    // subtasks form one contiguous queue range: pass 0 counts per job, then
+    // pass 1 writes job after job behind one allocation cursor.
+    b->job_split.assign(njobs, 0);
+    b->sub_off.assign(njobs, 0); b->sub_m.assign(njobs, 0);
+    if ((e = b->nsub.ensure((size_t)std::max<int64_t>(b->m, 1) * sizeof(uint32_t))) != cudaSuccess) break;
+    DevBuf sctr;
+    if ((e = sctr.ensure((size_t)(njobs + 1) * 16)) != cudaSuccess) break;
+    unsigned long long* sc = (unsigned long long*)sctr.p;   // [2j] subtasks of job j, [2*njobs+1] cursor
+    if ((e = cudaMemsetAsync(sc, 0, (size_t)(njobs + 1) * 16, st)) != cudaSuccess) { sctr.release(); break; }
+    for (int j = 0; j < njobs && e == cudaSuccess; j++) {
+      const int64_t lanes = resident_lanes(h, true, b->job_maxt[j]);
+      b->job_split[j] = (jobs[j].N <= 12) ? 0 : (h->split >= 0 ? h->split : choose_split(b->job_m[j], lanes));
+      e = launch_split(0, b->job_split[j], b->job_off[j], b->job_m[j], ta, (uint32_t*)b->nsub.p, nullptr, nullptr,
+                       sc + 2 * j, nullptr, nullptr, 0, st);
+    }
+    std::vector<unsigned long long> cnts((size_t)(njobs + 1) * 2, 0);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(cnts.data(), sc, cnts.size() * 8, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) { sctr.release(); break; }
+    int64_t total_sub = 0;
+    for (int j = 0; j < njobs; j++) { b->sub_off[j] = total_sub; b->sub_m[j] = (int64_t)cnts[2 * j]; total_sub += b->sub_m[j]; }
+    b->ms = total_sub;
+    if ((e = b->sroot.ensure((size_t)std::max<int64_t>(total_sub, 1) * sizeof(uint4))) != cudaSuccess ||
+        (e = b->sinfo.ensure((size_t)std::max<int64_t>(total_sub, 1) * sizeof(uint2))) != cudaSuccess) { sctr.release(); break; }
+    // settled counts of small tasks land in the control block's totals (zeroed above)
+    for (int j = 0; j < njobs && e == cudaSuccess; j++)
+      e = launch_split(1, b->job_split[j], b->job_off[j], b->job_m[j], ta, (uint32_t*)b->nsub.p, (uint4*)b->sroot.p,
+                       (uint2*)b->sinfo.p, sc + 2 * njobs, nullptr, (unsigned long long*)c, 0, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(b->h_out, c, cb, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    sctr.release();
+    if (e != cudaSuccess) break;
+    for (int j = 0; j < njobs; j++) b->fixed_total[j] += b->h_out[j];
+    b->device_bytes = (int64_t)(b->root.cap + b->info.cap + b->sched.cap + b->rec.cap + b->ctrl.cap + b->nsub.cap +
+                                b->sroot.cap + b->sinfo.cap);
   } while (0);
   if (e != cudaSuccess) status = h->cuda_fail(e, "batch build");
   if (status != NQ_OK) { nq_batch_destroy(b); return status; }
@@ -639,14 +724,14 @@ int nq_batch_run_plain(nq_batch* b, uint64_t* totals) {
   NQ_CUDA(h, cudaSetDevice(h->device));
   for (int j = 0; j < nj; j++) {
     uint64_t t = 0;
-    if (b->job_m[j] > 0) {
+    if (b->sub_m[j] > 0) {
       NQ_CUDA(h, cudaMemsetAsync(c, 0, 16, b->stream));
       TaskArrays ta;
-      ta.root = (uint4*)b->root.p + b->job_off[j]; ta.info = (uint2*)b->info.p + b->job_off[j];
-      ta.sched = (uint2*)b->sched.p + (size_t)b->job_off[j] * b->sw; ta.sw = b->sw; ta.wide = true;
-      // One job per launch: its tasks carry job id j, which lands in slot 0.
+      ta.root = (uint4*)b->root.p; ta.info = (uint2*)b->info.p; ta.sched = b->sched.p; ta.sw = b->sw; ta.wide = true;
+      // One job per launch over its subtask range; its tasks carry job id j, which lands in slot 0.
       DfsLaunch L;
-      L.tasks = ta; L.m = b->job_m[j]; L.cursor = (unsigned int*)(c + 8);
+      L.tasks = ta; L.sroot = (const uint4*)b->sroot.p + b->sub_off[j]; L.sinfo = (const uint2*)b->sinfo.p + b->sub_off[j];
+      L.m = b->sub_m[j]; L.cursor = (unsigned int*)(c + 8);
       L.job_totals = (unsigned long long*)c; L.job_base = (uint32_t)j; L.err = (unsigned int*)(c + 12);
       L.maxt = b->job_maxt[j]; L.block = b->block; L.grid = b->grid;
       NQ_CUDA(h, launch_dfs(L, b->stream));

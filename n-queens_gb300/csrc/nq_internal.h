@@ -25,7 +25,9 @@ struct TaskArrays {
 
 struct DfsLaunch {
   TaskArrays tasks;
-  int64_t m = 0;                        // number of tasks in the queue
+  const uint4* sroot = nullptr;         // split queue: subtask frames ...
+  const uint2* sinfo = nullptr;         // ... and {task, depth}; nullptr: the queue holds tasks
+  int64_t m = 0;                        // queue length
   const uint32_t* order = nullptr;      // optional queue order (task index per slot)
   unsigned int* cursor = nullptr;       // queue cursor (device, zeroed before launch)
   unsigned long long* job_totals = nullptr;  // weighted totals, slot (job id - job_base) (device)
@@ -44,6 +46,14 @@ cudaError_t launch_prepare(int N, int64_t m, const uint4* records, const TaskArr
                            uint32_t job, unsigned int* err, cudaStream_t st);
 
 cudaError_t launch_dfs(const DfsLaunch& L, cudaStream_t st);
+
+// Split tasks t0..t0+m-1 to depth D (0..3; 0 queues the tasks themselves).
+// pass 0: nsub[t] and ctr[0] += subtasks; pass 1: writes subtasks at the
+// allocation cursor ctr[1], initialises per_task (nullable) and adds counts
+// settled above depth D to job_totals.
+cudaError_t launch_split(int pass, int D, int64_t t0, int64_t m, const TaskArrays& ta, uint32_t* nsub, uint4* sroot,
+                         uint2* sinfo, unsigned long long* ctr, unsigned long long* per_task,
+                         unsigned long long* job_totals, uint32_t job_base, cudaStream_t st);
 
 // Largest block count per SM for a given stack depth (occupancy query).
 int dfs_blocks_per_sm(bool wide, int block, int maxt);

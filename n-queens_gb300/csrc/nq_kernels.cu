@@ -90,14 +90,152 @@ cudaError_t launch_prepare(int N, int64_t m, const uint4* records, const TaskArr
 }
 
 // ---------------------------------------------------------------------------
+// Schedule word decoding shared by the split and DFS kernels
+// ---------------------------------------------------------------------------
+struct Dec { uint32_t s, la, ra, fc, term, b14, tall; };
+__device__ __forceinline__ Dec decode(uint32_t w) {
+  return Dec{w >> C_SSHIFT, w & C_LA, w & C_RA, w & C_FC, w & C_TERM, w & C_B14, w & C_TALL};
+}
+__device__ __forceinline__ Dec decode(uint2 w) {
+  return Dec{(w.x >> W_SSHIFT) & 7u, w.x & W_LA, w.y, w.x & W_FC, w.x & W_TERM, w.x & W_B14, w.x & W_TALL};
+}
+
+// ---------------------------------------------------------------------------
+// split: expand every task to depth D (1..3) so the DFS queue holds many
+// small subtasks instead of few large ones (the reference's measured
+// bottleneck is the tail of large tasks, 14Bit_codon_GPU/README.md:4344-4404).
+// Pass 0 counts each task's depth-D frames into nsub[t] and the grand total
+// into ctr[0]; pass 1 writes them (warp-aggregated allocation on ctr[1]) and
+// settles, without subtasks, tasks that end above depth D and tasks whose
+// root is already terminal: their weighted count goes to per_task[t] (which
+// pass 1 initialises for every task) and to the job totals.
+// ---------------------------------------------------------------------------
+template <bool WIDE, int D>
+__global__ void __launch_bounds__(256) split_kernel(int pass, int64_t t0, int64_t m, const uint4* __restrict__ root,
+                                                    const uint2* __restrict__ info,
+                                                    const typename WordT<WIDE>::type* __restrict__ sched, int sw,
+                                                    uint32_t* __restrict__ nsub, uint4* __restrict__ sroot,
+                                                    uint2* __restrict__ sinfo, unsigned long long* ctr,
+                                                    unsigned long long* __restrict__ per_task,
+                                                    unsigned long long* job_totals, uint32_t job_base) {
+  const int64_t tr = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t t = t0 + tr;          // absolute task index
+  const unsigned lane = threadIdx.x & 31u;
+  const bool active = tr < m;
+  uint32_t count = 0;                 // depth-D frames of this task
+  unsigned long long direct = 0;      // unweighted count settled here
+  uint32_t wexp = 0, job = job_base;
+  uint32_t base = 0;
+  if (pass == 1) {
+    // reserve this warp's slots: exclusive scan of the per-task counts
+    const uint32_t mine = active ? nsub[t] : 0u;
+    uint32_t incl = mine;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t v = __shfl_up_sync(FULL, incl, o);
+      if ((int)lane >= o) incl += v;
+    }
+    const uint32_t tot = __shfl_sync(FULL, incl, 31);
+    unsigned long long wb = 0;
+    if (lane == 31 && tot) wb = atomicAdd(ctr + 1, (unsigned long long)tot);
+    wb = __shfl_sync(FULL, wb, 31);
+    base = (uint32_t)wb + incl - mine;
+  }
+  if (active) {
+    const uint2 in = info[t];
+    const uint32_t T = info_T(in.x);
+    wexp = info_wexp(in.x);
+    job = in.y;
+    if (T == INFO_NO_DFS || info_status(in.x) != TS_OK) {
+      direct = info_status(in.x) == TS_OK ? info_root(in.x) : 0u;
+    } else if (D == 0) {
+      if (pass == 1) { sroot[base] = root[t]; sinfo[base] = make_uint2((uint32_t)t, 0u); }
+      count = 1;
+    } else {
+      const uint32_t bm = (1u << info_N(in.x)) - 1u;
+      const typename WordT<WIDE>::type* w = sched + (size_t)t * sw;
+      uint4 st[D + 1];
+      st[0] = root[t];
+      int k = 0;
+      while (k >= 0) {
+        uint4& f = st[k];
+        if (f.w == 0u) { --k; continue; }
+        const uint32_t bit = f.w & (0u - f.w);
+        f.w ^= bit;
+        const Dec o = decode(w[k]);
+        const uint32_t nld = ((f.x | bit) << o.s) | o.la;
+        const uint32_t nrd = ((f.y | bit) >> o.s) | o.ra;
+        const uint32_t ncol = f.z | bit;
+        uint32_t nf = bm & ~(nld | nrd | ncol);
+        if (o.fc && (bm & ~((nld << 1) | (nrd >> 1) | ncol)) == 0u) nf = 0;
+        if (o.term) { direct += ((nf & (o.b14 ? ~1u : ~0u)) != 0u || o.tall) ? 1u : 0u; continue; }
+        if (nf == 0u) continue;
+        if (k + 1 == D) {
+          if (pass == 1) {
+            sroot[base + count] = make_uint4(nld, nrd, ncol, nf);
+            sinfo[base + count] = make_uint2((uint32_t)t, (uint32_t)D);
+          }
+          ++count;
+        } else {
+          st[k + 1] = make_uint4(nld, nrd, ncol, nf);
+          ++k;
+        }
+      }
+    }
+  }
+  if (pass == 0) {
+    if (active) nsub[t] = count;
+    uint32_t v = count;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+    if (lane == 0 && v) atomicAdd(ctr, (unsigned long long)v);
+    return;
+  }
+  const unsigned long long dv = direct << wexp;
+  if (active && per_task) per_task[t] = dv;
+  // job totals: one atomic per warp when the warp's tasks share a job
+  const uint32_t j0 = __shfl_sync(FULL, job, 0);
+  if (__all_sync(FULL, !active || job == j0)) {
+    unsigned long long v = active ? dv : 0ull;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+    if (lane == 0 && v) atomicAdd(job_totals + (j0 - job_base), v);
+  } else if (active && dv) {
+    atomicAdd(job_totals + (job - job_base), dv);
+  }
+}
+
+cudaError_t launch_split(int pass, int D, int64_t t0, int64_t m, const TaskArrays& ta, uint32_t* nsub, uint4* sroot,
+                         uint2* sinfo, unsigned long long* ctr, unsigned long long* per_task,
+                         unsigned long long* job_totals, uint32_t job_base, cudaStream_t st) {
+  if (m <= 0) return cudaSuccess;
+  const int B = 256;
+  const unsigned G = (unsigned)((m + B - 1) / B);
+#define NQ_SPLIT(WD, DD)                                                                                             \
+  split_kernel<WD, DD><<<G, B, 0, st>>>(pass, t0, m, ta.root, ta.info, (const typename WordT<WD>::type*)ta.sched, \
+                                        ta.sw, nsub, sroot, sinfo, ctr, per_task, job_totals, job_base)
+  if (ta.wide) {
+    if (D == 0) NQ_SPLIT(true, 0); else if (D == 1) NQ_SPLIT(true, 1); else if (D == 2) NQ_SPLIT(true, 2);
+    else NQ_SPLIT(true, 3);
+  } else {
+    if (D == 0) NQ_SPLIT(false, 0); else if (D == 1) NQ_SPLIT(false, 1); else if (D == 2) NQ_SPLIT(false, 2);
+    else NQ_SPLIT(false, 3);
+  }
+#undef NQ_SPLIT
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // DFS
 // ---------------------------------------------------------------------------
 struct DfsArgs {
-  const uint4* root;
+  const uint4* root;          // task roots (when sinfo == nullptr the queue holds tasks)
   const uint2* info;
   const void* sched;
   int sw;
-  int64_t m;
+  const uint4* sroot;         // subtask frames and {task, depth} (split queue)
+  const uint2* sinfo;
+  int64_t m;                  // queue length
   const uint32_t* order;
   unsigned int* cursor;
   unsigned long long* job_totals;
@@ -115,7 +253,7 @@ template <bool WIDE, int BLOCK>
 __global__ void __launch_bounds__(BLOCK) dfs_kernel(const DfsArgs a) {
   using W = typename WordT<WIDE>::type;
   extern __shared__ __align__(16) unsigned char smem[];
-  uint4* stk = reinterpret_cast<uint4*>(smem) + threadIdx.x;                             // stride BLOCK
+  uint4* stk = reinterpret_cast<uint4*>(smem) + threadIdx.x;                                   // stride BLOCK
   W* sch = reinterpret_cast<W*>(smem + (size_t)a.maxt * BLOCK * sizeof(uint4)) + threadIdx.x;  // stride BLOCK
   const unsigned lane = threadIdx.x & 31u;
   const unsigned lt_mask = (1u << lane) - 1u;
@@ -123,58 +261,66 @@ __global__ void __launch_bounds__(BLOCK) dfs_kernel(const DfsArgs a) {
 
   uint32_t ld = 0, rd = 0, col = 0, avail = 0, bm = 0;
   uint32_t d = 0, sp = 0;
-  unsigned long long cnt = 0;   // unweighted count of the current task
+  unsigned long long cnt = 0;   // unweighted count of the current (sub)task
   uint32_t wexp = 0, job = a.job_base;
-  int64_t task = -1;
+  uint32_t task = 0;
   bool have = false, exhausted = false;
   unsigned long long acc = 0;   // weighted count not yet flushed
   uint32_t acc_job = a.job_base;
 
   for (;;) {
     const bool idle = (avail == 0) && (sp == 0);
-    if (idle && have) {
-      const unsigned long long v = cnt << wexp;
-      if (a.per_task) a.per_task[task] = v;
-      if (job != acc_job) { flush_job(a, acc_job, acc); acc = 0; acc_job = job; }
-      acc += v;
-      have = false;
-    }
-    const bool want = idle && !exhausted;
-    const unsigned need = __ballot_sync(FULL, want);
-    if (need) {
-      const int leader = __ffs(need) - 1;
-      unsigned base = 0;
-      if ((int)lane == leader) base = atomicAdd(a.cursor, (unsigned)__popc(need));
-      base = __shfl_sync(FULL, base, leader);
-      if (want) {
-        const uint64_t slot = (uint64_t)base + (uint64_t)__popc(need & lt_mask);
-        if (slot < (uint64_t)a.m) {
-          const uint32_t t = a.order ? a.order[slot] : (uint32_t)slot;
-          const uint4 r = a.root[t];
-          const uint2 in = a.info[t];
-          const uint32_t T = info_T(in.x);
-          task = t; have = true;
-          cnt = info_root(in.x);
-          wexp = info_wexp(in.x);
-          job = in.y;
-          bm = (1u << info_N(in.x)) - 1u;
-          d = 0; sp = 0;
-          if (T == INFO_NO_DFS || info_status(in.x) != TS_OK) {
-            avail = 0;
-          } else if ((int)T > a.maxt) {      // frames at depths 0..T-1, words 0..T
-            atomicOr(a.err, DERR_DEPTH);
-            avail = 0;
+    if (__ballot_sync(FULL, idle)) {          // some lane finished: flush, refill, maybe exit
+      if (idle && have) {
+        const unsigned long long v = cnt << wexp;
+        if (a.per_task) {
+          if (a.sinfo) atomicAdd(a.per_task + task, v);
+          else a.per_task[task] = v;
+        }
+        if (job != acc_job) { flush_job(a, acc_job, acc); acc = 0; acc_job = job; }
+        acc += v;
+        have = false;
+      }
+      const bool want = idle && !exhausted;
+      const unsigned need = __ballot_sync(FULL, want);
+      if (need) {
+        const int leader = __ffs(need) - 1;
+        unsigned base = 0;
+        if ((int)lane == leader) base = atomicAdd(a.cursor, (unsigned)__popc(need));
+        base = __shfl_sync(FULL, base, leader);
+        if (want) {
+          const uint64_t slot = (uint64_t)base + (uint64_t)__popc(need & lt_mask);
+          if (slot < (uint64_t)a.m) {
+            const uint32_t q = a.order ? a.order[slot] : (uint32_t)slot;
+            uint4 r;
+            uint32_t d0;
+            if (a.sinfo) { const uint2 si = a.sinfo[q]; task = si.x; d0 = si.y; r = a.sroot[q]; }
+            else { task = q; d0 = 0; r = a.root[q]; }
+            const uint2 in = a.info[task];
+            const uint32_t T = info_T(in.x);
+            have = true;
+            cnt = (d0 == 0) ? info_root(in.x) : 0ull;
+            wexp = info_wexp(in.x);
+            job = in.y;
+            bm = (1u << info_N(in.x)) - 1u;
+            d = 0; sp = 0;
+            if (T == INFO_NO_DFS || info_status(in.x) != TS_OK || T < d0) {
+              avail = 0;
+            } else if ((int)(T - d0) > a.maxt) {    // frames at depths 0..T'-1, words 0..T'
+              atomicOr(a.err, DERR_DEPTH);
+              avail = 0;
+            } else {
+              ld = r.x; rd = r.y; col = r.z; avail = r.w;
+              const W* src = gsched + (size_t)task * a.sw + d0;
+              for (uint32_t k = 0; k <= T - d0; k++) sch[k * BLOCK] = src[k];
+            }
           } else {
-            ld = r.x; rd = r.y; col = r.z; avail = r.w;
-            const W* src = gsched + (size_t)t * a.sw;
-            for (uint32_t k = 0; k <= T; k++) sch[k * BLOCK] = src[k];
+            exhausted = true;
           }
-        } else {
-          exhausted = true;
         }
       }
+      if (__all_sync(FULL, exhausted && avail == 0 && sp == 0)) break;
     }
-    if (__all_sync(FULL, exhausted && avail == 0 && sp == 0)) break;
 
     if (avail == 0 && sp != 0) {          // resume the nearest saved frame
       --sp;
@@ -186,23 +332,15 @@ __global__ void __launch_bounds__(BLOCK) dfs_kernel(const DfsArgs a) {
     if (avail != 0) {                     // expand one candidate queen
       const uint32_t bit = avail & (0u - avail);
       avail ^= bit;
-      const W w = sch[d * BLOCK];
-      uint32_t s, la, ra, fc, term, b14, tall;
-      if constexpr (WIDE) {
-        s = (w.x >> W_SSHIFT) & 7u; la = w.x & W_LA; ra = w.y;
-        fc = w.x & W_FC; term = w.x & W_TERM; b14 = w.x & W_B14; tall = w.x & W_TALL;
-      } else {
-        s = w >> C_SSHIFT; la = w & C_LA; ra = w & C_RA;
-        fc = w & C_FC; term = w & C_TERM; b14 = w & C_B14; tall = w & C_TALL;
-      }
-      const uint32_t nld = ((ld | bit) << s) | la;
-      const uint32_t nrd = ((rd | bit) >> s) | ra;
+      const Dec o = decode(sch[d * BLOCK]);
+      const uint32_t nld = ((ld | bit) << o.s) | o.la;
+      const uint32_t nrd = ((rd | bit) >> o.s) | o.ra;
       const uint32_t ncol = col | bit;
       uint32_t nf = bm & ~(nld | nrd | ncol);
-      if (fc && (bm & ~((nld << 1) | (nrd >> 1) | ncol)) == 0u) nf = 0;
-      if (term) {
-        const uint32_t tm = b14 ? ~1u : ~0u;
-        cnt += ((nf & tm) != 0u || tall) ? 1ull : 0ull;
+      if (o.fc && (bm & ~((nld << 1) | (nrd >> 1) | ncol)) == 0u) nf = 0;
+      if (o.term) {
+        const uint32_t tm = o.b14 ? ~1u : ~0u;
+        cnt += ((nf & tm) != 0u || o.tall) ? 1ull : 0ull;
       } else if (nf != 0u) {
         if (avail != 0u) { stk[sp * BLOCK] = make_uint4(ld, rd, col, avail | (d << 27)); ++sp; }
         ld = nld; rd = nrd; col = ncol; avail = nf; ++d;
@@ -244,8 +382,9 @@ static cudaError_t launch_dfs_t(const DfsLaunch& L, cudaStream_t st) {
   }
   DfsArgs a;
   a.root = L.tasks.root; a.info = L.tasks.info; a.sched = L.tasks.sched; a.sw = L.tasks.sw;
-  a.m = L.m; a.order = L.order; a.cursor = L.cursor; a.job_totals = L.job_totals; a.job_base = L.job_base; a.per_task = L.per_task;
-  a.err = L.err; a.maxt = L.maxt;
+  a.sroot = L.sroot; a.sinfo = L.sinfo;
+  a.m = L.m; a.order = L.order; a.cursor = L.cursor; a.job_totals = L.job_totals; a.job_base = L.job_base;
+  a.per_task = L.per_task; a.err = L.err; a.maxt = L.maxt;
   dfs_kernel<WIDE, BLOCK><<<grid, BLOCK, smem, st>>>(a);
   return cudaGetLastError();
 }

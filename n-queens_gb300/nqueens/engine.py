@@ -202,16 +202,18 @@ class Batch:
 class Engine:
     """One CUDA device and stream of libnqgpu.so."""
 
-    def __init__(self, device: int = 0, block: int = 128, grid: int = 0, order_mode: int = 0):
+    def __init__(self, device: int = 0, block: int = 128, grid: int = 0, split: int = -1):
         h = ctypes.c_void_p()
         _check(lib().nq_create(ctypes.byref(h), int(device)), what=f"nq_create(device={device})")
         self._h = h
         self.device = device
-        self.set_config(block, grid, order_mode)
+        self.set_config(block, grid, split)
 
     # -- configuration ---------------------------------------------------
-    def set_config(self, block: int = 128, grid: int = 0, order_mode: int = 0) -> None:
-        _check(lib().nq_set_config(self._h, block, grid, order_mode), self._h, "set_config")
+    def set_config(self, block: int = 128, grid: int = 0, split: int = -1) -> None:
+        """Threads per block (64/128/256), grid (0: one wave of resident blocks) and split depth
+        (-1: automatic, 0..3: expand every task that many levels before the DFS)."""
+        _check(lib().nq_set_config(self._h, block, grid, split), self._h, "set_config")
 
     def get_config(self) -> Tuple[int, int, int]:
         b, g, o = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
@@ -245,6 +247,12 @@ class Engine:
         v = ctypes.c_double()
         _check(lib().nq_int32_peak(self._h, int(kind), ctypes.byref(v)), self._h, "int32_peak")
         return v.value
+
+    def last_run_info(self) -> Tuple[int, int]:
+        """(split depth, DFS queue length) of the last exec call."""
+        d, q = ctypes.c_int(), ctypes.c_int64()
+        _check(lib().nq_last_run_info(self._h, ctypes.byref(d), ctypes.byref(q)), self._h, "last_run_info")
+        return d.value, q.value
 
     def last_kernel_ms(self) -> Tuple[float, float]:
         """(prepare_ms, dfs_ms) of the last exec call, from CUDA events on its stream."""
@@ -305,16 +313,17 @@ def exec_solutions(N: int, constellations: List[Dict[str, int]], use_gpu: bool =
 
     Writes c["solutions"] = count x symmetry weight for every constellation.
     gpu_block selects threads per block (64/128/256) and gpu_max_blocks the
-    grid (0: one wave of resident blocks); gpu_sort_mode > 0 orders the queue
-    by estimated cost.  use_gpu=False is rejected: this engine has no CPU
+    grid (0: one wave of resident blocks); the reference's reorder knobs
+    (gpu_sort_mode and the rest) are accepted and ignored, since the queue is
+    balanced by splitting.  use_gpu=False is rejected: this engine has no CPU
     path."""
     if not use_gpu:
         raise ValueError("the GB300 engine has no CPU path (use_gpu=False is the reference's own CPU branch)")
     if not constellations:
         return
     eng = default_engine()
-    eng.set_config(gpu_block if gpu_block in (64, 128, 256) else 128, max(0, int(gpu_max_blocks)),
-                   1 if gpu_sort_mode > 0 else 0)
+    _, _, split = eng.get_config()
+    eng.set_config(gpu_block if gpu_block in (64, 128, 256) else 128, max(0, int(gpu_max_blocks)), split)
     recs = records_from_constellations(constellations)
     total, sol = eng.exec_records(N, recs, want_solutions=True)
     for c, v in zip(constellations, sol.tolist()):

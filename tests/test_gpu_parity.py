@@ -131,13 +131,30 @@ def test_ragged_and_duplicated_records(eng, oracle_mod):
 @pytest.mark.parametrize("block", [64, 128, 256])
 def test_launch_configs_agree(eng, oracle_mod, block):
     import nqueens
-    eng.set_config(block, 0, 0)
+    eng.set_config(block, 0, -1)
     try:
         assert eng.count(16).total == oracle_mod.EXPECTED_TOTAL[16]
-        eng.set_config(block, 37, 0)   # a grid that is not a multiple of anything
+        eng.set_config(block, 37, -1)   # a grid that is not a multiple of anything
         assert eng.count(14).total == oracle_mod.EXPECTED_TOTAL[14]
     finally:
-        eng.set_config(128, 0, 0)
+        eng.set_config(128, 0, -1)
+
+
+@pytest.mark.parametrize("split", [0, 1, 2, 3])
+def test_split_depths_per_record(eng, oracle_mod, split):
+    """Per-record counts are the same whatever the split depth (subtask counts are summed per record)."""
+    import nqueens
+    eng.set_config(128, 0, split)
+    try:
+        for N in (8, 13, 15):
+            recs = nqueens.gen_records(N)
+            total, sol = eng.exec_records(N, recs, want_solutions=True)
+            want = oracle_mod.exec_solutions(N, _o_records(oracle_mod, recs))
+            assert np.array_equal(sol, want), (N, split)
+            assert total == oracle_mod.EXPECTED_TOTAL[N]
+        assert eng.count(17).total == oracle_mod.EXPECTED_TOTAL[17]
+    finally:
+        eng.set_config(128, 0, -1)
 
 
 def _queens(rng, N, k):
