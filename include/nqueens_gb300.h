@@ -92,6 +92,25 @@ int nq_last_kernel_ms(nq_handle *h, float *prepare_ms, float *dfs_ms);
  * DFS queue it built (records, or subtasks when split). */
 int nq_last_run_info(const nq_handle *h, int *split_depth, int64_t *queued);
 
+/* exec_solutions for callers that cannot allocate device memory -- no
+ * counterpart in the reference.  Some callers must not call cudaMalloc or
+ * cudaFree once running: a serving process whose device memory is owned by
+ * another allocator or a fixed budget, or a latency-critical loop where an
+ * allocation's implicit device synchronisation would stall other streams.
+ * Same inputs and outputs as nq_exec_solutions_device (device records in,
+ * device per-record counts (nullable) and total out, on `stream`, NULL = the
+ * legacy default stream), but no handle and no allocation of any kind: the
+ * scratch is one fixed __device__ array of about 15 MiB inside the library,
+ * held by every GPU that loads it until exit.  Limit: m <= 131072 records and
+ * schedules up to 24 depths (N - start_min <= 25); larger inputs are rejected
+ * with NQ_EINVAL, never truncated.  No task splitting.  The first call on each
+ * device looks the array's address up (cudaGetSymbolAddress) with that device
+ * current; make that first call before any stream capture.  Every call shares
+ * the one array, so calls that overlap on the GPU race: serialise them.  The
+ * call waits for its stream and returns the device status. */
+int nq_exec_solutions_noalloc(int N, const nq_record *d_records, int64_t m, int start_min, uint64_t *d_solutions,
+                              uint64_t *d_total, void *stream);
+
 /* Whole-board total for N, the loop body of the reference's main()
  * (356Py_savesp_narrow.py:6036-6046): brute force on the GPU for N <= 5
  * (the reference's _bit_total, :5755-5767), the constellation path above.

@@ -69,6 +69,7 @@ SIGNATURES = {
     "nq_exec_solutions": (ctypes.c_int, [_vp, ctypes.c_int, _vp, ctypes.c_int64, _u64p, _u64p]),
     "nq_exec_solutions_device": (ctypes.c_int, [_vp, ctypes.c_int, _vp, ctypes.c_int64, ctypes.c_int, _vp, _vp,
                                                 _vp]),
+    "nq_exec_solutions_noalloc": (ctypes.c_int, [ctypes.c_int, _vp, ctypes.c_int64, ctypes.c_int, _vp, _vp, _vp]),
     "nq_sync": (ctypes.c_int, [_vp]),
     "nq_last_run_info": (ctypes.c_int, [_vp, _ip, ctypes.POINTER(ctypes.c_int64)]),
     "nq_last_kernel_ms": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
