@@ -159,7 +159,7 @@ int run_records(nq_handle* h, int N, const uint4* d_rec, int64_t m, int start_mi
   const int D = h->split >= 0 ? h->split : choose_split(m, resident_lanes(h, false, maxt));
   DfsLaunch L;
   L.tasks = ta; L.m = m; L.order = nullptr; L.cursor = cursor; L.job_totals = totals;
-  L.per_task = d_per_task; L.err = err; L.maxt = maxt; L.block = h->block; L.grid = h->grid;
+  L.per_task = d_per_task; L.err = err; L.maxt = maxt; L.block = h->block; L.grid = h->grid; L.big = N >= 24;
   if (D > 0) {
     NQ_CUDA(h, h->nsub.ensure((size_t)m * sizeof(uint32_t)));
     NQ_CUDA(h, launch_split(0, D, 0, m, ta, (uint32_t*)h->nsub.p, nullptr, nullptr, sctr, nullptr, totals, 0, st));
@@ -455,6 +455,7 @@ struct nq_batch {
   int64_t m = 0;        // tasks
   int64_t ms = 0;       // queued subtasks (every job's split output, job after job)
   int maxt = 1, sw = 2, grid = 0, block = 128;
+  bool big = false;                        // some job has N >= 24: u64 per-task counters
   std::vector<int64_t> job_off, job_m;     // task range per job
   std::vector<int64_t> sub_off, sub_m;     // subtask range per job
   std::vector<int> job_maxt, job_split;
@@ -481,7 +482,7 @@ int batch_enqueue(nq_batch* b, int use_graph) {
     L.tasks = ta; L.sroot = (const uint4*)b->sroot.p; L.sinfo = (const uint2*)b->sinfo.p;
     L.m = b->ms; L.cursor = (unsigned int*)(c + (size_t)nj * 8);
     L.job_totals = (unsigned long long*)c; L.err = (unsigned int*)(c + (size_t)nj * 8 + 4);
-    L.maxt = b->maxt; L.block = b->block; L.grid = b->grid;
+    L.maxt = b->maxt; L.block = b->block; L.grid = b->grid; L.big = b->big;
     e = launch_dfs(L, st);
     if (e != cudaSuccess) return e;
     return cudaMemcpyAsync(b->h_out, c, cb, cudaMemcpyDeviceToHost, st);
@@ -590,6 +591,7 @@ int nq_batch_create(nq_handle* h, const nq_job* jobs, int njobs, nq_batch** out)
   }
   if (maxt >= kMaxDepth) { nq_batch_destroy(b); return h->fail(NQ_ESTACK, "batch: schedule too deep"); }
   b->maxt = maxt; b->sw = maxt + 1;
+  for (int j = 0; j < njobs; j++) b->big = b->big || jobs[j].N >= 24;
   const int64_t m_rec = (int64_t)recs.size(), m_host = (int64_t)htasks.size();
   b->m = m_rec + m_host;
   for (auto& sg : segs) { b->job_off[sg.job] = sg.rec_off; b->job_m[sg.job] = sg.m; }
@@ -733,7 +735,7 @@ int nq_batch_run_plain(nq_batch* b, uint64_t* totals) {
       L.tasks = ta; L.sroot = (const uint4*)b->sroot.p + b->sub_off[j]; L.sinfo = (const uint2*)b->sinfo.p + b->sub_off[j];
       L.m = b->sub_m[j]; L.cursor = (unsigned int*)(c + 8);
       L.job_totals = (unsigned long long*)c; L.job_base = (uint32_t)j; L.err = (unsigned int*)(c + 12);
-      L.maxt = b->job_maxt[j]; L.block = b->block; L.grid = b->grid;
+      L.maxt = b->job_maxt[j]; L.block = b->block; L.grid = b->grid; L.big = b->jobs[j].N >= 24;
       NQ_CUDA(h, launch_dfs(L, b->stream));
       NQ_CUDA(h, cudaMemcpyAsync(b->h_out, c, 16, cudaMemcpyDeviceToHost, b->stream));
       NQ_CUDA(h, cudaStreamSynchronize(b->stream));

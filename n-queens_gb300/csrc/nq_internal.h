@@ -35,6 +35,7 @@ struct DfsLaunch {
   unsigned long long* per_task = nullptr;    // optional weighted count per task (device)
   unsigned int* err = nullptr;          // device error word
   int maxt = 0;                         // stack frames per lane (>= T of every task; words: maxt+1)
+  bool big = false;                     // u64 per-task counters (some task has N >= 24)
   int block = 128;
   int grid = 0;                         // 0: one wave of resident blocks
 };

@@ -19,6 +19,8 @@
 //   shared memory, interleaved by lane so every access is conflict-free.
 //   Counts are summed per lane in u64 and flushed per job with one atomicAdd
 //   per warp (shuffle tree) at exit or per task when the job id changes.
+#include <type_traits>
+
 #include "nq_common.cuh"
 #include "nq_internal.h"
 
@@ -249,7 +251,52 @@ __device__ __forceinline__ void flush_job(const DfsArgs& a, unsigned job, unsign
   if (v) atomicAdd(a.job_totals + (job - a.job_base), v);
 }
 
-template <bool WIDE, int BLOCK>
+size_t dfs_smem_bytes(bool wide, int block, int maxt) {
+  return (size_t)block * ((size_t)maxt * sizeof(uint4) + (size_t)(maxt + 1) * (wide ? 8 : 4));
+}
+
+// One lane's DFS state and its step.  Every lane runs the same predicated
+// sequence each step: resume a saved frame if the current one is exhausted,
+// take the lowest candidate, build the child with the depth's schedule word,
+// apply the look-ahead, then count (terminal depth) or descend.  '+' replaces
+// '|' where the bits are disjoint (a candidate is never in ld, rd or col),
+// so those adds issue on the FMA pipe as well as the ALU pipe.  Per-task
+// counts are u32 (BIG: u64, for N >= 24, where one task may pass 2^32).
+template <bool WIDE, bool BIG>
+struct Lane {
+  uint32_t ld = 0, rd = 0, col = 0, avail = 0, bm = 0, d = 0, sp = 0;
+  typename std::conditional<BIG, unsigned long long, uint32_t>::type cnt = 0;
+
+  template <int BLOCK>
+  __device__ __forceinline__ void step(uint4* stk, const typename WordT<WIDE>::type* sch) {
+    if (avail == 0 && sp != 0) {
+      --sp;
+      const uint4 f = stk[sp * BLOCK];
+      ld = f.x; rd = f.y; col = f.z;
+      avail = f.w & 0x07FFFFFFu;
+      d = f.w >> 27;
+    }
+    const bool act = avail != 0;
+    const uint32_t bit = avail & (0u - avail);
+    avail -= bit;
+    const Dec o = decode(sch[d * BLOCK]);
+    const uint32_t nld = ((ld + bit) << o.s) | o.la;
+    const uint32_t nrd = ((rd + bit) >> o.s) | o.ra;
+    const uint32_t ncol = col + bit;
+    uint32_t nf = bm & ~(nld | nrd | ncol);
+    const uint32_t ahead = bm & ~((nld + nld) | (nrd >> 1) | ncol);
+    if (ahead == 0u && o.fc) nf = 0;
+    const uint32_t tm = o.term ? (o.b14 ? ~1u : ~0u) : 0u;   // terminal: count instead of descend
+    bool hit = (nf & tm) != 0u;
+    if constexpr (WIDE) hit = hit || (o.term && o.tall);
+    cnt += (act && hit) ? 1u : 0u;
+    const bool desc = act && tm == 0u && nf != 0u;
+    if (desc && avail != 0u) { stk[sp * BLOCK] = make_uint4(ld, rd, col, avail | (d << 27)); ++sp; }
+    if (desc) { ld = nld; rd = nrd; col = ncol; avail = nf; ++d; }
+  }
+};
+
+template <bool WIDE, int BLOCK, bool BIG>
 __global__ void __launch_bounds__(BLOCK) dfs_kernel(const DfsArgs a) {
   using W = typename WordT<WIDE>::type;
   extern __shared__ __align__(16) unsigned char smem[];
@@ -258,21 +305,17 @@ __global__ void __launch_bounds__(BLOCK) dfs_kernel(const DfsArgs a) {
   const unsigned lane = threadIdx.x & 31u;
   const unsigned lt_mask = (1u << lane) - 1u;
   const W* __restrict__ gsched = reinterpret_cast<const W*>(a.sched);
-
-  uint32_t ld = 0, rd = 0, col = 0, avail = 0, bm = 0;
-  uint32_t d = 0, sp = 0;
-  unsigned long long cnt = 0;   // unweighted count of the current (sub)task
-  uint32_t wexp = 0, job = a.job_base;
-  uint32_t task = 0;
+  Lane<WIDE, BIG> L;
+  uint32_t wexp = 0, job = a.job_base, task = 0;
   bool have = false, exhausted = false;
-  unsigned long long acc = 0;   // weighted count not yet flushed
+  unsigned long long acc = 0;
   uint32_t acc_job = a.job_base;
 
   for (;;) {
-    const bool idle = (avail == 0) && (sp == 0);
+    const bool idle = (L.avail | L.sp) == 0u;
     if (__ballot_sync(FULL, idle)) {          // some lane finished: flush, refill, maybe exit
       if (idle && have) {
-        const unsigned long long v = cnt << wexp;
+        const unsigned long long v = (unsigned long long)L.cnt << wexp;
         if (a.per_task) {
           if (a.sinfo) atomicAdd(a.per_task + task, v);
           else a.per_task[task] = v;
@@ -299,18 +342,18 @@ __global__ void __launch_bounds__(BLOCK) dfs_kernel(const DfsArgs a) {
             const uint2 in = a.info[task];
             const uint32_t T = info_T(in.x);
             have = true;
-            cnt = (d0 == 0) ? info_root(in.x) : 0ull;
+            L.cnt = (d0 == 0) ? info_root(in.x) : 0u;
             wexp = info_wexp(in.x);
             job = in.y;
-            bm = (1u << info_N(in.x)) - 1u;
-            d = 0; sp = 0;
+            L.bm = (1u << info_N(in.x)) - 1u;
+            L.d = 0; L.sp = 0;
             if (T == INFO_NO_DFS || info_status(in.x) != TS_OK || T < d0) {
-              avail = 0;
+              L.avail = 0;
             } else if ((int)(T - d0) > a.maxt) {    // frames at depths 0..T'-1, words 0..T'
               atomicOr(a.err, DERR_DEPTH);
-              avail = 0;
+              L.avail = 0;
             } else {
-              ld = r.x; rd = r.y; col = r.z; avail = r.w;
+              L.ld = r.x; L.rd = r.y; L.col = r.z; L.avail = r.w;
               const W* src = gsched + (size_t)task * a.sw + d0;
               for (uint32_t k = 0; k <= T - d0; k++) sch[k * BLOCK] = src[k];
             }
@@ -319,36 +362,12 @@ __global__ void __launch_bounds__(BLOCK) dfs_kernel(const DfsArgs a) {
           }
         }
       }
-      if (__all_sync(FULL, exhausted && avail == 0 && sp == 0)) break;
+      if (__all_sync(FULL, exhausted && (L.avail | L.sp) == 0u)) break;
     }
-
-    if (avail == 0 && sp != 0) {          // resume the nearest saved frame
-      --sp;
-      const uint4 f = stk[sp * BLOCK];
-      ld = f.x; rd = f.y; col = f.z;
-      avail = f.w & 0x07FFFFFFu;
-      d = f.w >> 27;
-    }
-    if (avail != 0) {                     // expand one candidate queen
-      const uint32_t bit = avail & (0u - avail);
-      avail ^= bit;
-      const Dec o = decode(sch[d * BLOCK]);
-      const uint32_t nld = ((ld | bit) << o.s) | o.la;
-      const uint32_t nrd = ((rd | bit) >> o.s) | o.ra;
-      const uint32_t ncol = col | bit;
-      uint32_t nf = bm & ~(nld | nrd | ncol);
-      if (o.fc && (bm & ~((nld << 1) | (nrd >> 1) | ncol)) == 0u) nf = 0;
-      if (o.term) {
-        const uint32_t tm = o.b14 ? ~1u : ~0u;
-        cnt += ((nf & tm) != 0u || o.tall) ? 1ull : 0ull;
-      } else if (nf != 0u) {
-        if (avail != 0u) { stk[sp * BLOCK] = make_uint4(ld, rd, col, avail | (d << 27)); ++sp; }
-        ld = nld; rd = nrd; col = ncol; avail = nf; ++d;
-      }
-    }
+    L.template step<BLOCK>(stk, sch);
+    L.template step<BLOCK>(stk, sch);
   }
 
-  // Flush: one atomic per warp when the warp's lanes share a job, else per lane.
   const uint32_t j0 = __shfl_sync(FULL, acc_job, 0);
   const bool same = __all_sync(FULL, acc == 0 || acc_job == j0);
   if (same) {
@@ -361,21 +380,17 @@ __global__ void __launch_bounds__(BLOCK) dfs_kernel(const DfsArgs a) {
   }
 }
 
-size_t dfs_smem_bytes(bool wide, int block, int maxt) {
-  return (size_t)block * ((size_t)maxt * sizeof(uint4) + (size_t)(maxt + 1) * (wide ? 8 : 4));
-}
-
-template <bool WIDE, int BLOCK>
+template <bool WIDE, int BLOCK, bool BIG>
 static cudaError_t launch_dfs_t(const DfsLaunch& L, cudaStream_t st) {
   const size_t smem = dfs_smem_bytes(WIDE, BLOCK, L.maxt);
-  cudaError_t e = cudaFuncSetAttribute(dfs_kernel<WIDE, BLOCK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = cudaFuncSetAttribute(dfs_kernel<WIDE, BLOCK, BIG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   int grid = L.grid;
   if (grid <= 0) {
     int dev = 0, sms = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, dfs_kernel<WIDE, BLOCK>, BLOCK, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, dfs_kernel<WIDE, BLOCK, BIG>, BLOCK, smem);
     if (e != cudaSuccess) return e;
     if (per <= 0) return cudaErrorInvalidConfiguration;
     grid = sms * per;
@@ -385,28 +400,35 @@ static cudaError_t launch_dfs_t(const DfsLaunch& L, cudaStream_t st) {
   a.sroot = L.sroot; a.sinfo = L.sinfo;
   a.m = L.m; a.order = L.order; a.cursor = L.cursor; a.job_totals = L.job_totals; a.job_base = L.job_base;
   a.per_task = L.per_task; a.err = L.err; a.maxt = L.maxt;
-  dfs_kernel<WIDE, BLOCK><<<grid, BLOCK, smem, st>>>(a);
+  dfs_kernel<WIDE, BLOCK, BIG><<<grid, BLOCK, smem, st>>>(a);
   return cudaGetLastError();
 }
+
 
 cudaError_t launch_dfs(const DfsLaunch& L, cudaStream_t st) {
   if (L.m <= 0) return cudaSuccess;
   if (L.maxt < 1 || L.maxt > kMaxDepth) return cudaErrorInvalidValue;
+#define NQ_DFS_BLOCK(B)                                                                        \
+  if (L.tasks.wide) return L.big ? launch_dfs_t<true, B, true>(L, st) : launch_dfs_t<true, B, false>(L, st); \
+  return L.big ? launch_dfs_t<false, B, true>(L, st) : launch_dfs_t<false, B, false>(L, st);
   switch (L.block) {
-    case 64: return L.tasks.wide ? launch_dfs_t<true, 64>(L, st) : launch_dfs_t<false, 64>(L, st);
-    case 128: return L.tasks.wide ? launch_dfs_t<true, 128>(L, st) : launch_dfs_t<false, 128>(L, st);
-    case 256: return L.tasks.wide ? launch_dfs_t<true, 256>(L, st) : launch_dfs_t<false, 256>(L, st);
+    case 64: { NQ_DFS_BLOCK(64) }
+    case 128: { NQ_DFS_BLOCK(128) }
+    case 256: { NQ_DFS_BLOCK(256) }
     default: return cudaErrorInvalidValue;
   }
+#undef NQ_DFS_BLOCK
 }
 
 template <bool WIDE, int BLOCK>
 static int occ(int maxt) {
   const size_t smem = dfs_smem_bytes(WIDE, BLOCK, maxt);
-  if (cudaFuncSetAttribute(dfs_kernel<WIDE, BLOCK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+  if (cudaFuncSetAttribute(dfs_kernel<WIDE, BLOCK, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+      cudaSuccess)
     return 0;
   int per = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, dfs_kernel<WIDE, BLOCK>, BLOCK, smem) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, dfs_kernel<WIDE, BLOCK, false>, BLOCK, smem) != cudaSuccess)
+    return 0;
   return per;
 }
 

@@ -90,6 +90,7 @@ extern "C" int nq_exec_solutions_noalloc(int N, const nq_record* d_records, int6
     DfsLaunch L;
     L.tasks = ta; L.m = m; L.cursor = cursor; L.job_totals = totals;
     L.per_task = (unsigned long long*)d_solutions; L.err = err; L.maxt = maxt; L.block = 128; L.grid = 0;
+    L.big = N >= 24;
     if (launch_dfs(L, st) != cudaSuccess) return NQ_ECUDA;
   }
   if (cudaMemcpyAsync(d_total, totals, 8, cudaMemcpyDeviceToDevice, st) != cudaSuccess) return NQ_ECUDA;

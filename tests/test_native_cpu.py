@@ -228,3 +228,4 @@ def test_completion_full_board(nq, oracle_mod):
 def test_exec_solutions_rejects_cpu_path(nq):
     with pytest.raises(ValueError):
         nq.exec_solutions(8, [{"ld": 0, "rd": 0, "col": 0, "startijkl": 0, "solutions": 0}], use_gpu=False)
+
