@@ -1,0 +1,61 @@
+"""Command line: the reference's per-N table, on the GB300 engine.
+
+    python -m nqueens [nmin nmax] [--repeat R] [--split D] [--block B] [--unique]
+
+prints, like the reference's main() (14Bit_codon_GPU/356Py_savesp_narrow.py:5899-6046),
+
+     N:             Total           Unique         hh:mm:ss.ms
+    19:        4968057848                0         0:00:00.152    ok
+
+for N in range(nmin, nmax), with "ok" / "ng(got!=expected)" against the
+reference's known-answer table (356Py_savesp_narrow.py:5775).  Unique is 0 on
+the constellation path, as in the reference, unless --unique is given.
+--repeat runs each count R times (the last one is printed), which is how
+profiles/ captures a warm kernel.
+"""
+from __future__ import annotations
+
+import argparse
+import datetime as dt
+import sys
+
+from .engine import Engine
+
+# Known totals, 356Py_savesp_narrow.py:5775 (index = N).
+EXPECTED = [0, 1, 0, 0, 2, 10, 4, 40, 92, 352, 724, 2680, 14200, 73712, 365596, 2279184, 14772512, 95815104,
+            666090624, 4968057848, 39029188884, 314666222712, 2691008701644, 24233937684440, 227514171973736,
+            2207893435808352, 22317699616364044, 234907967154122528]
+
+
+def _fmt(td: dt.timedelta) -> str:
+    return str(td)[:-3] if td.microseconds else str(td) + ".000"
+
+
+def main(argv=None) -> int:
+    ap = argparse.ArgumentParser(prog="python -m nqueens", description=__doc__.split("\n")[0])
+    ap.add_argument("nmin", nargs="?", type=int, default=5)
+    ap.add_argument("nmax", nargs="?", type=int, default=20, help="exclusive upper bound, as range()")
+    ap.add_argument("--repeat", type=int, default=1)
+    ap.add_argument("--split", type=int, default=-1)
+    ap.add_argument("--block", type=int, default=128)
+    ap.add_argument("--device", type=int, default=0)
+    ap.add_argument("--unique", action="store_true", help="also count unique solutions (symmetry method)")
+    a = ap.parse_args(argv)
+    eng = Engine(a.device, block=a.block, split=a.split)
+    print(" N:             Total           Unique         hh:mm:ss.ms")
+    rc = 0
+    for N in range(a.nmin, a.nmax):
+        for _ in range(max(1, a.repeat)):
+            t0 = dt.datetime.now()
+            r = eng.count_unique(N) if a.unique and hasattr(eng, "count_unique") else eng.count(N)
+            el = dt.datetime.now() - t0
+        status = "ok" if N < len(EXPECTED) and EXPECTED[N] == r.total else f"ng({r.total}!={EXPECTED[N]})"
+        if status != "ok":
+            rc = 1
+        print(f"{N:2d}:{r.total:18d}{r.unique:17d}{_fmt(el):>21s}    {status}", flush=True)
+    eng.close()
+    return rc
+
+
+if __name__ == "__main__":
+    sys.exit(main())
