@@ -306,6 +306,121 @@ def ours_arm(args):
     return 0
 
 
+def batch_arm(args):
+    """Config: 256 counting jobs, N uniform in 10..18 from numpy default_rng(2026), tasks resident,
+    all in one graph-captured persistent launch vs one launch and read-back per job."""
+    import numpy as np
+    import torch
+    import nqueens
+    rng = np.random.default_rng(2026)
+    Ns = [int(x) for x in rng.integers(10, 19, size=256)]
+    eng = nqueens.Engine(0, block=args.block)
+    want = [eng.count(N).total for N in sorted(set(Ns))]
+    want = dict(zip(sorted(set(Ns)), want))
+    t0 = time.perf_counter()
+    b = eng.batch([nqueens.CountJob(N) for N in Ns])
+    build_s = time.perf_counter() - t0
+    exp = np.array([want[N] for N in Ns], np.uint64)
+    for _ in range(args.warmup):
+        assert np.array_equal(b.run(use_graph=True), exp)
+        assert np.array_equal(b.run_plain(), exp)
+    t_graph, t_plain = [], []
+    for _ in range(args.steps):
+        t0 = time.perf_counter(); r = b.run(use_graph=True); t_graph.append(time.perf_counter() - t0)
+        assert np.array_equal(r, exp)
+        t0 = time.perf_counter(); r = b.run_plain(); t_plain.append(time.perf_counter() - t0)
+        assert np.array_equal(r, exp)
+    # drop-in per job: nq_count (host generation, upload, prepare, split, DFS, read-back) for every job
+    t0 = time.perf_counter()
+    for N in Ns:
+        assert eng.count(N).total == want[N]
+    dropin_s = time.perf_counter() - t0
+    g, p = statistics.mean(t_graph), statistics.mean(t_plain)
+    # where batching pays: a mix of small boards (N uniform 6..14), launch-bound in the plain form
+    small_Ns = [int(x) for x in np.random.default_rng(2026).integers(6, 15, size=256)]
+    sb = eng.batch([nqueens.CountJob(N) for N in small_Ns])
+    sexp = np.array([eng.count(N).total for N in small_Ns], np.uint64)
+    assert np.array_equal(sb.run(use_graph=True), sexp) and np.array_equal(sb.run_plain(), sexp)
+    sg, sp = [], []
+    for _ in range(max(3, args.steps)):
+        t0 = time.perf_counter(); sb.run(use_graph=True); sg.append(time.perf_counter() - t0)
+        t0 = time.perf_counter(); sb.run_plain(); sp.append(time.perf_counter() - t0)
+    sb.close()
+    small = {"jobs": 256, "N": "uniform 6..14", "graph_jobs_per_s": 256 / statistics.mean(sg),
+             "plain_resident_jobs_per_s": 256 / statistics.mean(sp),
+             "speedup_vs_plain_resident": statistics.mean(sp) / statistics.mean(sg)}
+    line = {"metric": "mixed-batch jobs/s (256 jobs, N~U{10..18})", "value": len(Ns) / g, "unit": "jobs/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * g, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+            "config": {"workload": "256 counting jobs, N uniform 10..18 (numpy default_rng(2026)), one graph-captured "
+                                   "persistent launch per step, tasks resident", "jobs": len(Ns),
+                       "tasks": b.tasks, "block": args.block},
+            "plain_resident_jobs_per_s": len(Ns) / p, "plain_resident_ms": 1e3 * p,
+            "speedup_vs_plain_resident": p / g,
+            "batch_build_s": build_s, "e2e": {"value": len(Ns) / (build_s + g), "unit": "jobs/s",
+                                              "h2d_bytes_per_step": None, "d2h_bytes_per_step": 8 * len(Ns)},
+            "plain_dropin_jobs_per_s": len(Ns) / dropin_s, "speedup_e2e_vs_dropin": dropin_s / (build_s + g),
+            "small_mix": small, "gpu_launches": 1}
+    b.close()
+    eng.close()
+    print(json.dumps(line))
+    return 0
+
+
+def serve_arm(args):
+    """Config: served completion stream -- N uniform 14..20, k uniform 0..4 pre-placed queens (seeded),
+    Poisson arrivals at a stated rate, admission by device-memory budget; vs the plain per-query launch."""
+    import numpy as np
+    import nqueens
+    from nqueens.server import Server, random_completion_queries, run_plain
+    jobs = random_completion_queries(args.queries, seed=2026, N_range=(14, 20), k_range=(0, 4))
+    rng = np.random.default_rng(7)
+    gaps = rng.exponential(1.0 / args.rate, size=len(jobs))
+    eng = nqueens.Engine(0, block=args.block)
+    run_plain(eng, jobs[:4])                         # warm-up (module load, allocations)
+    # plain: one query at a time, FIFO, same arrival times
+    arrivals = np.cumsum(gaps)
+    t_start = time.perf_counter()
+    lat_plain, res_plain = [], []
+    for j, a in zip(jobs, arrivals):
+        now = time.perf_counter() - t_start
+        if now < a:
+            time.sleep(a - now)
+        r = run_plain(eng, [j])[0]
+        res_plain.append(r)
+        lat_plain.append(time.perf_counter() - t_start - a)
+    span_plain = time.perf_counter() - t_start
+    with Server(engine=eng, budget_bytes=args.budget_gb << 30, max_inflight=args.inflight,
+                max_batch_jobs=args.max_batch) as srv:
+        t_start = time.perf_counter()
+        futs = []
+        for j, a in zip(jobs, arrivals):
+            now = time.perf_counter() - t_start
+            if now < a:
+                time.sleep(a - now)
+            futs.append(srv.submit(j))
+        srv.drain(600)
+        res_srv = [f.result() for f in futs]
+        st = srv.stats()
+    assert res_srv == res_plain, "served counts differ from the plain per-query counts"
+    eng.close()
+    pl = np.array(lat_plain)
+    line = {"metric": "served completion stream jobs/s (N~U{14..20}, k~U{0..4})", "value": st.jobs_per_s,
+            "unit": "jobs/s", "n_gpus": 1, "steps": 1, "warmup": 1, "ms_per_step": 1e3 * st.makespan_s,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+            "config": {"workload": f"{len(jobs)} queries, Poisson arrivals {args.rate}/s (numpy default_rng(2026) "
+                                   "boards, default_rng(7) gaps), continuous batching",
+                       "budget_gb": args.budget_gb, "max_inflight": args.inflight, "max_batch_jobs": args.max_batch},
+            "p50_ms": 1e3 * st.percentile(50), "p99_ms": 1e3 * st.percentile(99), "batches": st.batches,
+            "max_inflight_seen": st.max_inflight_seen,
+            "plain": {"jobs_per_s": len(jobs) / span_plain, "p50_ms": 1e3 * float(np.percentile(pl, 50)),
+                      "p99_ms": 1e3 * float(np.percentile(pl, 99))},
+            "e2e": {"value": st.jobs_per_s, "unit": "jobs/s", "h2d_bytes_per_step": None, "d2h_bytes_per_step": None},
+            "exact": True}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -316,9 +431,20 @@ def main():
     ap.add_argument("--split", type=int, default=-1, help="split depth (-1 automatic)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", choices=["n19", "batch", "serve"], default="n19",
+                    help="n19: the headline single-N count; batch / serve: the batching and serving configs")
+    ap.add_argument("--queries", type=int, default=150)
+    ap.add_argument("--rate", type=float, default=10.0, help="serve: Poisson arrival rate (queries/s)")
+    ap.add_argument("--budget-gb", type=int, default=32)
+    ap.add_argument("--inflight", type=int, default=3)
+    ap.add_argument("--max-batch", type=int, default=16)
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
+    if args.workload == "batch":
+        return batch_arm(args)
+    if args.workload == "serve":
+        return serve_arm(args)
     return ours_arm(args)
 
 

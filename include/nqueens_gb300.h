@@ -157,6 +157,12 @@ typedef struct nq_batch nq_batch;
 /* Builds every job's tasks, uploads them once and keeps them resident. */
 int nq_batch_create(nq_handle *h, const nq_job *jobs, int njobs, nq_batch **out);
 int64_t nq_batch_tasks(const nq_batch *b);
+/* Grid of the batch's persistent launch (0 = one wave of resident blocks on the
+ * whole GPU).  A smaller grid leaves SMs to batches running beside it. */
+int nq_batch_set_grid(nq_batch *b, int grid);
+/* Resident DFS blocks on the whole GPU for the handle's block size and a stack
+ * of maxt frames (wide: batch schedule words). */
+int nq_resident_blocks(nq_handle *h, int wide, int maxt, int *blocks);
 int64_t nq_batch_device_bytes(const nq_batch *b);
 /* All jobs in one persistent launch (use_graph: replay a captured CUDA graph). */
 int nq_batch_run(nq_batch *b, int use_graph, uint64_t *totals);

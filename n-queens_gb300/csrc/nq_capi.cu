@@ -8,6 +8,8 @@
 
 #include <algorithm>
 #include <chrono>
+#include <map>
+#include <mutex>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -25,18 +27,25 @@ using namespace nq;
 
 namespace {
 
+// Device buffer.  With a stream set, allocation and release are stream-ordered
+// (cudaMallocAsync / cudaFreeAsync on that stream), so building or freeing one
+// batch never waits for kernels of other batches still running.
 struct DevBuf {
   void* p = nullptr;
   size_t cap = 0;
+  cudaStream_t ordered = nullptr;
   cudaError_t ensure(size_t n) {
     if (n <= cap) return cudaSuccess;
-    if (p) { cudaFree(p); p = nullptr; cap = 0; }
+    release();
     size_t want = std::max<size_t>(n, 256);
-    cudaError_t e = cudaMalloc(&p, want);
-    if (e == cudaSuccess) cap = want;
+    cudaError_t e = ordered ? cudaMallocAsync(&p, want, ordered) : cudaMalloc(&p, want);
+    if (e == cudaSuccess) cap = want; else p = nullptr;
     return e;
   }
-  void release() { if (p) cudaFree(p); p = nullptr; cap = 0; }
+  void release() {
+    if (p) { if (ordered) cudaFreeAsync(p, ordered); else cudaFree(p); }
+    p = nullptr; cap = 0;
+  }
 };
 
 // Control block of one run: totals (u64 per job), queue cursor, error word.
@@ -94,6 +103,35 @@ struct nq_handle {
   DevBuf rec, root, info, sched, per_task, ctrl, nsub, sroot, sinfo;
   uint64_t* h_ctrl = nullptr;   // pinned read-back of the control block
   size_t h_ctrl_cap = 0;
+  // pinned read-back blocks for batches, reused (freeing pinned memory can
+  // synchronise the device, which would stall other batches in flight)
+  std::mutex pin_mu;
+  std::vector<std::pair<void*, size_t>> pin_free;
+  void* pin_get(size_t bytes) {
+    {
+      std::lock_guard<std::mutex> lk(pin_mu);
+      for (size_t i = 0; i < pin_free.size(); i++)
+        if (pin_free[i].second >= bytes) {
+          void* q = pin_free[i].first;
+          pin_free.erase(pin_free.begin() + (long)i);
+          pinned_sizes[q] = bytes;
+          return q;
+        }
+    }
+    const size_t want = std::max<size_t>(bytes, 65536);
+    void* q = nullptr;
+    if (cudaMallocHost(&q, want) != cudaSuccess) return nullptr;
+    std::lock_guard<std::mutex> lk(pin_mu);
+    pinned_cap[q] = want;
+    pinned_sizes[q] = bytes;
+    return q;
+  }
+  void pin_put(void* q) {
+    if (!q) return;
+    std::lock_guard<std::mutex> lk(pin_mu);
+    pin_free.push_back({q, pinned_cap[q]});
+  }
+  std::map<void*, size_t> pinned_cap, pinned_sizes;
   bool pending = false;
   int last_split = 0;        // split depth and queue length of the last run
   int64_t last_queue = 0;
@@ -238,6 +276,7 @@ void nq_destroy(nq_handle* h) {
   h->rec.release(); h->root.release(); h->info.release(); h->sched.release(); h->per_task.release(); h->ctrl.release();
   h->nsub.release(); h->sroot.release(); h->sinfo.release();
   if (h->h_ctrl) cudaFreeHost(h->h_ctrl);
+  for (auto& q : h->pinned_cap) cudaFreeHost(q.first);
   for (auto& e : h->ev) if (e) cudaEventDestroy(e);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
@@ -456,6 +495,7 @@ struct nq_batch {
   int64_t ms = 0;       // queued subtasks (every job's split output, job after job)
   int maxt = 1, sw = 2, grid = 0, block = 128;
   bool big = false;                        // some job has N >= 24: u64 per-task counters
+  bool wide = true;                        // 8-byte schedule words (completion tasks); compact otherwise
   std::vector<int64_t> job_off, job_m;     // task range per job
   std::vector<int64_t> sub_off, sub_m;     // subtask range per job
   std::vector<int> job_maxt, job_split;
@@ -464,6 +504,10 @@ struct nq_batch {
   cudaGraphExec_t graph = nullptr;
   bool submitted = false;
   int64_t device_bytes = 0;
+  cudaError_t set_ordered() {
+    for (DevBuf* d : {&rec, &root, &info, &sched, &ctrl, &nsub, &sroot, &sinfo}) d->ordered = stream;
+    return cudaSuccess;
+  }
 };
 
 namespace {
@@ -477,7 +521,7 @@ int batch_enqueue(nq_batch* b, int use_graph) {
     cudaError_t e = cudaMemsetAsync(c, 0, cb, st);
     if (e != cudaSuccess) return e;
     TaskArrays ta;
-    ta.root = (uint4*)b->root.p; ta.info = (uint2*)b->info.p; ta.sched = b->sched.p; ta.sw = b->sw; ta.wide = true;
+    ta.root = (uint4*)b->root.p; ta.info = (uint2*)b->info.p; ta.sched = b->sched.p; ta.sw = b->sw; ta.wide = b->wide;
     DfsLaunch L;
     L.tasks = ta; L.sroot = (const uint4*)b->sroot.p; L.sinfo = (const uint2*)b->sinfo.p;
     L.m = b->ms; L.cursor = (unsigned int*)(c + (size_t)nj * 8);
@@ -531,7 +575,8 @@ void nq_batch_destroy(nq_batch* b) {
   if (b->graph) cudaGraphExecDestroy(b->graph);
   b->rec.release(); b->root.release(); b->info.release(); b->sched.release(); b->ctrl.release();
   b->nsub.release(); b->sroot.release(); b->sinfo.release();
-  if (b->h_out) cudaFreeHost(b->h_out);
+  if (b->stream) cudaStreamSynchronize(b->stream);   // this batch's own frees only
+  b->h->pin_put(b->h_out);
   if (b->done) cudaEventDestroy(b->done);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
@@ -591,6 +636,7 @@ int nq_batch_create(nq_handle* h, const nq_job* jobs, int njobs, nq_batch** out)
   }
   if (maxt >= kMaxDepth) { nq_batch_destroy(b); return h->fail(NQ_ESTACK, "batch: schedule too deep"); }
   b->maxt = maxt; b->sw = maxt + 1;
+  b->wide = !htasks.empty();             // constellation-only batches keep the compact 4-byte words
   for (int j = 0; j < njobs; j++) b->big = b->big || jobs[j].N >= 24;
   const int64_t m_rec = (int64_t)recs.size(), m_host = (int64_t)htasks.size();
   b->m = m_rec + m_host;
@@ -601,11 +647,13 @@ int nq_batch_create(nq_handle* h, const nq_job* jobs, int njobs, nq_batch** out)
   cudaError_t e;
   if ((e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking)) != cudaSuccess ||
       (e = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming)) != cudaSuccess ||
-      (e = cudaMallocHost((void**)&b->h_out, cb)) != cudaSuccess ||
+      (e = b->set_ordered()) != cudaSuccess ||
+      (e = ((b->h_out = (uint64_t*)h->pin_get(cb)) ? cudaSuccess : cudaErrorMemoryAllocation)) != cudaSuccess ||
       (e = b->ctrl.ensure(cb)) != cudaSuccess ||
       (e = b->root.ensure((size_t)std::max<int64_t>(b->m, 1) * sizeof(uint4))) != cudaSuccess ||
       (e = b->info.ensure((size_t)std::max<int64_t>(b->m, 1) * sizeof(uint2))) != cudaSuccess ||
-      (e = b->sched.ensure((size_t)std::max<int64_t>(b->m, 1) * b->sw * sizeof(uint2))) != cudaSuccess ||
+      (e = b->sched.ensure((size_t)std::max<int64_t>(b->m, 1) * b->sw * (b->wide ? sizeof(uint2) : sizeof(uint32_t)))) !=
+          cudaSuccess ||
       (e = b->rec.ensure((size_t)std::max<int64_t>(m_rec, 1) * sizeof(nq_record))) != cudaSuccess) {
     int st = h->cuda_fail(e, "batch allocation");
     nq_batch_destroy(b);
@@ -613,7 +661,7 @@ int nq_batch_create(nq_handle* h, const nq_job* jobs, int njobs, nq_batch** out)
   }
   b->device_bytes = (int64_t)(b->root.cap + b->info.cap + b->sched.cap + b->rec.cap + b->ctrl.cap);
   TaskArrays ta;
-  ta.root = (uint4*)b->root.p; ta.info = (uint2*)b->info.p; ta.sched = b->sched.p; ta.sw = b->sw; ta.wide = true;
+  ta.root = (uint4*)b->root.p; ta.info = (uint2*)b->info.p; ta.sched = b->sched.p; ta.sw = b->sw; ta.wide = b->wide;
   unsigned char* c = (unsigned char*)b->ctrl.p;
   unsigned int* derr = (unsigned int*)(c + (size_t)njobs * 8 + 4);
   cudaStream_t st = b->stream;
@@ -651,11 +699,12 @@ int nq_batch_create(nq_handle* h, const nq_job* jobs, int njobs, nq_batch** out)
     b->sub_off.assign(njobs, 0); b->sub_m.assign(njobs, 0);
     if ((e = b->nsub.ensure((size_t)std::max<int64_t>(b->m, 1) * sizeof(uint32_t))) != cudaSuccess) break;
     DevBuf sctr;
+    sctr.ordered = st;
     if ((e = sctr.ensure((size_t)(njobs + 1) * 16)) != cudaSuccess) break;
     unsigned long long* sc = (unsigned long long*)sctr.p;   // [2j] subtasks of job j, [2*njobs+1] cursor
     if ((e = cudaMemsetAsync(sc, 0, (size_t)(njobs + 1) * 16, st)) != cudaSuccess) { sctr.release(); break; }
     for (int j = 0; j < njobs && e == cudaSuccess; j++) {
-      const int64_t lanes = resident_lanes(h, true, b->job_maxt[j]);
+      const int64_t lanes = resident_lanes(h, b->wide, b->job_maxt[j]);
       b->job_split[j] = (jobs[j].N <= 12) ? 0 : (h->split >= 0 ? h->split : choose_split(b->job_m[j], lanes));
       e = launch_split(0, b->job_split[j], b->job_off[j], b->job_m[j], ta, (uint32_t*)b->nsub.p, nullptr, nullptr,
                        sc + 2 * j, nullptr, nullptr, 0, st);
@@ -684,6 +733,20 @@ int nq_batch_create(nq_handle* h, const nq_job* jobs, int njobs, nq_batch** out)
   if (e != cudaSuccess) status = h->cuda_fail(e, "batch build");
   if (status != NQ_OK) { nq_batch_destroy(b); return status; }
   *out = b;
+  return NQ_OK;
+}
+
+int nq_batch_set_grid(nq_batch* b, int grid) {
+  if (!b || grid < 0) return NQ_EINVAL;
+  if (b->submitted) return b->h->fail(NQ_EBUSY, "batch is running");
+  if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }   // the captured launch used the old grid
+  b->grid = grid;
+  return NQ_OK;
+}
+
+int nq_resident_blocks(nq_handle* h, int wide, int maxt, int* blocks) {
+  if (!h || !blocks || maxt < 1 || maxt >= kMaxDepth) return NQ_EINVAL;
+  *blocks = h->sms * std::max(1, dfs_blocks_per_sm(wide != 0, h->block, maxt));
   return NQ_OK;
 }
 
@@ -729,7 +792,7 @@ int nq_batch_run_plain(nq_batch* b, uint64_t* totals) {
     if (b->sub_m[j] > 0) {
       NQ_CUDA(h, cudaMemsetAsync(c, 0, 16, b->stream));
       TaskArrays ta;
-      ta.root = (uint4*)b->root.p; ta.info = (uint2*)b->info.p; ta.sched = b->sched.p; ta.sw = b->sw; ta.wide = true;
+      ta.root = (uint4*)b->root.p; ta.info = (uint2*)b->info.p; ta.sched = b->sched.p; ta.sw = b->sw; ta.wide = b->wide;
       // One job per launch over its subtask range; its tasks carry job id j, which lands in slot 0.
       DfsLaunch L;
       L.tasks = ta; L.sroot = (const uint4*)b->sroot.p + b->sub_off[j]; L.sinfo = (const uint2*)b->sinfo.p + b->sub_off[j];

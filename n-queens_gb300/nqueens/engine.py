@@ -166,6 +166,10 @@ class Batch:
     def device_bytes(self) -> int:
         return int(lib().nq_batch_device_bytes(self._b))
 
+    def set_grid(self, grid: int) -> None:
+        """Blocks of this batch's persistent launch (0: every resident block of the GPU)."""
+        _check(lib().nq_batch_set_grid(self._b, int(grid)), self.engine._h, "batch set_grid")
+
     def run(self, use_graph: bool = True) -> np.ndarray:
         """All jobs in one persistent launch; per-job uint64 totals."""
         _check(lib().nq_batch_run(self._b, int(use_graph), _lib.p64(self._totals)), self.engine._h, "batch run")
@@ -275,6 +279,12 @@ class Engine:
         _check(lib().nq_count_completions(self._h, int(N), len(q), rows, cols, _lib.p64(t)), self._h,
                f"count_completions(N={N})")
         return int(t[0])
+
+    def resident_blocks(self, wide: bool = True, maxt: int = 18) -> int:
+        """DFS blocks resident on the whole GPU at this block size and stack depth."""
+        v = ctypes.c_int()
+        _check(lib().nq_resident_blocks(self._h, int(wide), int(maxt), ctypes.byref(v)), self._h, "resident_blocks")
+        return v.value
 
     def batch(self, jobs: Iterable) -> Batch:
         return Batch(self, list(jobs))

@@ -1,0 +1,319 @@
+"""Continuous-batching request loop (no reference counterpart: the reference
+counts one N per process run).
+
+Requests -- whole-board counts (``CountJob``) and completion queries with
+pre-placed queens (``CompletionJob``) -- are queued as they arrive and sorted
+into two lanes by their estimated GPU time.  Large requests (a whole N=20
+board, say) each get a batch of their own whose persistent kernel holds most
+of the resident blocks; small requests that arrive meanwhile are gathered
+into batches on the remaining share of the GPU, so they never queue behind a
+large one.  A scheduler thread admits a lane's queued requests as a new
+batch whenever that lane has a free slot and the device-memory budget allows:
+the batch's tasks are built and uploaded (``nq_batch_create``), then launched
+asynchronously on the batch's own CUDA stream (``nq_batch_submit``), so
+batches admitted while others run overlap them on the GPU.  Finished batches
+are polled (bounded waits), their per-job totals resolve the requests'
+futures, and their device memory returns to the budget.
+
+Counts are exact integers: a request's result is the same alone and in any
+mix (tests/test_server.py checks it).  Each request records its latency
+(arrival to result); ``stats()`` reports p50/p99 and jobs/s.
+"""
+from __future__ import annotations
+
+import collections
+import threading
+import time
+from concurrent.futures import Future
+from dataclasses import dataclass, field
+from typing import Deque, List, Optional, Sequence
+
+import numpy as np
+
+from ._lib import NQError
+from .engine import Batch, CompletionJob, CountJob, Engine
+
+
+@dataclass
+class _Request:
+    job: object
+    future: Future
+    t_arrival: float
+    t_done: float = 0.0
+
+
+@dataclass
+class _InFlight:
+    batch: Batch
+    requests: List[_Request]
+    bytes: int
+    large: bool = False
+
+
+# GPU milliseconds of a whole-board count on GB300 (measured with bench-style timing).
+_COUNT_MS = {16: 1.4, 17: 5.4, 18: 26.0, 19: 143.0, 20: 1190.0, 21: 9500.0}
+
+
+def estimate_ms(job) -> float:
+    """Rough GPU time of a request: a whole board from the table above; k pre-placed
+    queens cut the unweighted search (8x the symmetric one) by about N per queen."""
+    N = job.N
+    base = _COUNT_MS.get(N, 0.5 if N < 16 else 80000.0)
+    if isinstance(job, CountJob):
+        return base
+    k = len(job.queens)
+    if k == 0:
+        return base * 8.0
+    return base * 8.0 / float(N) ** k
+
+
+def _bytes_estimate(job) -> int:
+    """Device bytes a job's tasks are expected to take, for admission before building."""
+    N = job.N
+    if isinstance(job, CountJob) and N >= 6:
+        tasks = {13: 7731, 14: 13233, 15: 21270, 16: 33046, 17: 49207, 18: 571705, 19: 897071,
+                 20: 1369061, 21: 2025282}.get(N, 200000 if N > 21 else 4300)
+        return tasks * (16 + 8 + 8 * N + 16) * 8      # tasks + split subtasks
+    return 4096 * N * (24 + 8 * (N + 1)) * 2
+
+
+@dataclass
+class ServerStats:
+    completed: int
+    latencies_s: List[float] = field(default_factory=list)
+    makespan_s: float = 0.0
+    batches: int = 0
+    max_inflight_seen: int = 0
+
+    def percentile(self, q: float) -> float:
+        return float(np.percentile(self.latencies_s, q)) if self.latencies_s else 0.0
+
+    @property
+    def jobs_per_s(self) -> float:
+        return self.completed / self.makespan_s if self.makespan_s > 0 else 0.0
+
+
+class Server:
+    """Admit requests into batches by device-memory budget and keep several batches in flight."""
+
+    def __init__(self, device: int = 0, budget_bytes: int = 16 << 30, max_inflight: int = 3,
+                 max_batch_jobs: int = 64, use_graph: bool = False, engine: Optional[Engine] = None,
+                 poll_us: int = 200, share_gpu: bool = True, large_ms: float = 10.0, large_share: float = 0.875):
+        self.engine = engine or Engine(device)
+        # Lanes: requests estimated above large_ms run one per batch on large_share of the
+        # resident blocks; the rest are batched on the remaining share (share_gpu), so a
+        # small request admitted while a large one runs starts at once beside it.
+        full = self.engine.resident_blocks()
+        self._grid_large = max(1, int(full * large_share)) if share_gpu else 0
+        self._grid_small = max(1, full - self._grid_large) if share_gpu else 0
+        self.large_ms = float(large_ms)
+        self.budget = int(budget_bytes)
+        self.max_inflight = int(max_inflight)
+        self.max_batch_jobs = int(max_batch_jobs)
+        self.use_graph = use_graph
+        self.poll_us = int(poll_us)
+        self._pending: Deque[_Request] = collections.deque()        # small requests
+        self._pending_large: Deque[_Request] = collections.deque()  # large requests
+        self._inflight: List[_InFlight] = []
+        self._building = 0
+        self._admitted = 0
+        self._cv = threading.Condition()
+        self._stop = False
+        self._done: List[_Request] = []
+        self._batches = 0
+        self._max_inflight_seen = 0
+        self._t0: Optional[float] = None
+        self._t_last = 0.0
+        self._error: Optional[BaseException] = None
+        self._thread = threading.Thread(target=self._loop, name="nqueens-server", daemon=True)
+        self._thread.start()
+
+    # -- client side ---------------------------------------------------------
+    def submit(self, job) -> Future:
+        if not isinstance(job, (CountJob, CompletionJob)):
+            raise TypeError("submit a CountJob or a CompletionJob")
+        f: Future = Future()
+        now = time.perf_counter()
+        with self._cv:
+            if self._error is not None:
+                raise RuntimeError("server stopped after an error") from self._error
+            if self._t0 is None:
+                self._t0 = now
+            r = _Request(job, f, now)
+            (self._pending_large if estimate_ms(job) > self.large_ms else self._pending).append(r)
+            self._cv.notify()
+        return f
+
+    def drain(self, timeout_s: float = 600.0) -> None:
+        """Wait until every submitted request has a result (bounded)."""
+        t_end = time.perf_counter() + timeout_s
+        with self._cv:
+            while self._pending or self._pending_large or self._inflight or self._building:
+                if self._error is not None:
+                    raise RuntimeError("server failed") from self._error
+                left = t_end - time.perf_counter()
+                if left <= 0:
+                    raise TimeoutError("requests still running after the drain timeout")
+                self._cv.wait(min(left, 0.05))
+
+    def stats(self) -> ServerStats:
+        with self._cv:
+            lat = [r.t_done - r.t_arrival for r in self._done]
+            span = (self._t_last - self._t0) if self._t0 is not None else 0.0
+            return ServerStats(len(self._done), lat, span, self._batches, self._max_inflight_seen)
+
+    def close(self) -> None:
+        with self._cv:
+            self._stop = True
+            self._cv.notify()
+        self._thread.join(timeout=60)
+        for f in self._inflight:
+            f.batch.close()
+        self._inflight.clear()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- scheduler thread ------------------------------------------------------
+    def _collect(self) -> bool:
+        progressed = False
+        for fl in list(self._inflight):
+            out = fl.batch.poll(0)
+            if out is None:
+                continue
+            now = time.perf_counter()
+            for r, v in zip(fl.requests, out.tolist()):
+                r.t_done = now
+                r.future.set_result(int(v))
+            fl.batch.close()
+            with self._cv:
+                self._inflight.remove(fl)
+                self._admitted -= fl.bytes
+                self._done.extend(fl.requests)
+                self._t_last = now
+                self._cv.notify_all()
+            progressed = True
+        return progressed
+
+    def _admit_lane(self, large: bool) -> bool:
+        queue = self._pending_large if large else self._pending
+        with self._cv:
+            n_lane = sum(1 for f in self._inflight if f.large == large)
+            slots = 1 if large else max(1, self.max_inflight - 1)
+            if not queue or n_lane >= slots:
+                return False
+            take: List[_Request] = []
+            est = 0
+            while queue and len(take) < (1 if large else self.max_batch_jobs):
+                e = _bytes_estimate(queue[0].job)
+                if take and self._admitted + est + e > self.budget:
+                    break
+                if not take and self._inflight and self._admitted + e > self.budget:
+                    return False          # wait for memory to free up
+                take.append(queue.popleft())
+                est += e
+            self._building += 1          # taken off the queue, not yet in flight
+        try:
+            batch = Batch(self.engine, [r.job for r in take])   # host build + upload, other batches keep running
+        except NQError as exc:
+            self._reject(take, exc, queue)
+            with self._cv:
+                self._building -= 1
+                self._cv.notify_all()
+            return True
+        nbytes = batch.device_bytes
+        grid = self._grid_large if large else self._grid_small
+        if grid:
+            batch.set_grid(grid)
+        batch.submit(self.use_graph)
+        with self._cv:
+            self._inflight.append(_InFlight(batch, take, nbytes, large))
+            self._building -= 1
+            self._admitted += nbytes
+            self._batches += 1
+            self._max_inflight_seen = max(self._max_inflight_seen, len(self._inflight))
+        return True
+
+    def _admit(self) -> bool:
+        a = self._admit_lane(True)
+        b = self._admit_lane(False)
+        return a or b
+
+    def _reject(self, take: List[_Request], exc: NQError, queue: Deque[_Request]) -> None:
+        """A batch failed to build: build its requests one by one so only the bad ones fail."""
+        for r in take:
+            if len(take) > 1:
+                try:
+                    b = Batch(self.engine, [r.job])
+                except NQError as e1:
+                    r.future.set_exception(e1)
+                    continue
+                b.close()
+                with self._cv:
+                    queue.appendleft(r)              # valid: queue it again
+            else:
+                r.future.set_exception(exc)
+
+    def _loop(self) -> None:
+        try:
+            while True:
+                with self._cv:
+                    idle = not self._pending and not self._pending_large and not self._inflight
+                    if self._stop and idle:
+                        return
+                    if idle:
+                        self._cv.wait(0.05)
+                        continue
+                progressed = self._collect()
+                progressed = self._admit() or progressed
+                if not progressed:
+                    time.sleep(self.poll_us * 1e-6)
+        except BaseException as exc:            # surface failures to the clients
+            with self._cv:
+                self._error = exc
+                for r in list(self._pending) + list(self._pending_large):
+                    r.future.set_exception(exc)
+                self._pending.clear()
+                self._pending_large.clear()
+                for fl in self._inflight:
+                    for r in fl.requests:
+                        if not r.future.done():
+                            r.future.set_exception(exc)
+                self._cv.notify_all()
+
+
+def random_completion_queries(n: int, seed: int, N_range=(14, 20), k_range=(0, 4)) -> List[object]:
+    """The served completion stream of the workload: N uniform in N_range, k uniform
+    in k_range pre-placed queens at seeded rows and columns, resampled while any two
+    attack each other.  k == 0 is a whole-board count (CountJob)."""
+    rng = np.random.default_rng(seed)
+    out: List[object] = []
+    for _ in range(n):
+        N = int(rng.integers(N_range[0], N_range[1] + 1))
+        k = int(rng.integers(k_range[0], k_range[1] + 1))
+        if k == 0:
+            out.append(CountJob(N))
+            continue
+        while True:
+            rows = rng.choice(N, size=k, replace=False)
+            cols = rng.integers(0, N, size=k)
+            q = list(zip(rows.tolist(), cols.tolist()))
+            if all(q[a][1] != q[b][1] and abs(q[a][0] - q[b][0]) != abs(q[a][1] - q[b][1])
+                   for a in range(k) for b in range(a + 1, k)):
+                break
+        out.append(CompletionJob(N, q))
+    return out
+
+
+def run_plain(engine: Engine, jobs: Sequence) -> List[int]:
+    """The plain form: one synchronous call (one launch sequence) per job, in order."""
+    res = []
+    for j in jobs:
+        if isinstance(j, CountJob):
+            res.append(engine.count(j.N, j.preset).total)
+        else:
+            res.append(engine.count_completions(j.N, j.queens))
+    return res

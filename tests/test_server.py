@@ -1,0 +1,65 @@
+"""Serving loop: every request's count is exact and the same alone and in the mix."""
+import time
+
+import numpy as np
+import pytest
+
+from conftest import gpu_available
+
+pytestmark = [pytest.mark.gpu, pytest.mark.skipif(not gpu_available(), reason="needs a CUDA GPU")]
+
+
+def _oracle_answer(oracle_mod, job):
+    import nqueens
+    if isinstance(job, nqueens.CountJob):
+        return oracle_mod.EXPECTED_TOTAL[job.N]
+    return oracle_mod.completions(job.N, [r for r, _ in job.queens], [c for _, c in job.queens])
+
+
+@pytest.mark.parametrize("share_gpu,max_inflight", [(True, 3), (False, 2), (True, 1)])
+def test_server_results_exact_and_same_as_alone(oracle_mod, share_gpu, max_inflight):
+    import nqueens
+    from nqueens.server import Server, random_completion_queries, run_plain
+    jobs = random_completion_queries(60, seed=11, N_range=(8, 13), k_range=(0, 4))
+    eng = nqueens.Engine(0)
+    try:
+        alone = run_plain(eng, jobs)
+        with Server(engine=eng, max_inflight=max_inflight, max_batch_jobs=7, share_gpu=share_gpu) as srv:
+            rng = np.random.default_rng(5)
+            futs = []
+            for j in jobs:                                  # staggered arrivals: batches overlap
+                futs.append(srv.submit(j))
+                time.sleep(float(rng.exponential(0.0005)))
+            srv.drain(120)
+            mixed = [f.result(timeout=10) for f in futs]
+            st = srv.stats()
+        assert mixed == alone
+        assert mixed == [_oracle_answer(oracle_mod, j) for j in jobs]
+        assert st.completed == len(jobs) and st.batches >= 2
+        assert 0 < st.percentile(50) <= st.percentile(99)
+    finally:
+        eng.close()
+
+
+def test_server_small_budget_still_exact(oracle_mod):
+    """A budget smaller than one batch admits one batch at a time; results stay exact."""
+    import nqueens
+    from nqueens.server import Server, random_completion_queries
+    jobs = random_completion_queries(20, seed=3, N_range=(10, 14), k_range=(1, 3))
+    with Server(budget_bytes=1, max_inflight=3, max_batch_jobs=4) as srv:
+        futs = [srv.submit(j) for j in jobs]
+        srv.drain(120)
+        got = [f.result(timeout=10) for f in futs]
+        assert srv.stats().max_inflight_seen == 1
+    assert got == [_oracle_answer(oracle_mod, j) for j in jobs]
+
+
+def test_server_rejects_bad_request():
+    import nqueens
+    from nqueens.server import Server
+    with Server(max_inflight=1) as srv:
+        with pytest.raises(TypeError):
+            srv.submit("N=8")
+        f = srv.submit(nqueens.CompletionJob(8, [(0, 0), (0, 0)]))   # the same queen twice: a bad argument
+        with pytest.raises(Exception):
+            f.result(timeout=30)
