@@ -117,6 +117,11 @@ int nq_exec_solutions_noalloc(int N, const nq_record *d_records, int64_t m, int 
  * preset <= 0 selects nq_preset_for(N). */
 int nq_count(nq_handle *h, int N, int preset, uint64_t *total);
 
+/* Unique (distinct under rotation and reflection) and total counts by the
+ * symmetry method (11Bit_Python/07Py_bit_symmetry.py:65-200; GPU form
+ * 10Bit_CUDA/01CUDA_Bit_Symmetry.cu:627-960).  4 <= N <= 27. */
+int nq_count_unique(nq_handle *h, int N, uint64_t *unique, uint64_t *total);
+
 /* Completions of a board with k pre-placed queens (rows[i], cols[i]; column c
  * is bit c): the number of full placements that contain them.  No reference
  * counterpart (the reference counts whole boards only); brute-force checked. */

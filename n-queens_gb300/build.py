@@ -24,7 +24,7 @@ OUT_DIR = os.path.join(HERE, "nqueens")
 LIB = os.path.join(OUT_DIR, "libnqgpu.so")
 OBJ_DIR = os.path.join(HERE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["nq_kernels.cu", "nq_capi.cu", "nq_host.cpp", "nq_noalloc.cu"]
+SOURCES = ["nq_kernels.cu", "nq_capi.cu", "nq_host.cpp", "nq_noalloc.cu", "nq_unique.cu"]
 
 
 def nvcc() -> str:

@@ -1,0 +1,314 @@
+// nq_unique.cu -- unique and total counts by the symmetry method on sm_103a.
+//
+// Restates the classic symmetry-elimination search of the reference
+// (11Bit_Python/07Py_bit_symmetry.py:65-200; GPU form 10Bit_CUDA/
+// 01CUDA_Bit_Symmetry.cu:627-960):
+//   * corner solutions: queen at row 0 column 0, row 1 at column bound1
+//     (2 <= bound1 <= N-2); rows below bound1 may not use column 1; every
+//     solution counts x8 (backTrack1, :152-170);
+//   * the rest: row 0 at column bound1 with bound2 = N-1-bound1 and
+//     bound1 < bound2; rows above bound1 avoid the side columns, row bound2 is
+//     gated on the side columns used so far, the last row must avoid lastmask
+//     (backTrack2, :126-151); each solution is classified by its rotations as
+//     x2, x4 or x8 or dropped as a non-canonical copy (symmetryops, :65-125).
+// Unique = c2 + c4 + c8, total = 2 c2 + 4 c4 + 8 c8.
+//
+// The host expands the first rows of every (part, bound1) start into tasks;
+// the kernel is persistent, queue-fed and explicit-stack like the
+// constellation DFS (one candidate per lane per step), keeping each lane's
+// board (one bit per row) in shared memory for the leaf classification.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "../../include/nqueens_gb300.h"
+#include "nq_common.cuh"
+#include "nq_internal.h"
+
+namespace nq {
+namespace {
+
+constexpr unsigned FULLM = 0xFFFFFFFFu;
+constexpr int kBoardWords = 8;   // rows of the board prefix carried by a task
+
+// One start configuration (symmetry part and its bounds).
+struct UConf {
+  uint32_t part;       // 1 corner, 2 no corner
+  uint32_t bound1, bound2, endbit, lastmask, sidemask, topbit;
+};
+
+// A task: the search state at `row` plus the board rows above it.
+struct UTask {
+  uint32_t left, down, right, avail;
+  uint32_t row, conf;
+  uint32_t board[kBoardWords];
+};
+
+// symmetryops (07Py_bit_symmetry.py:65-125): 2, 4 or 8 for a canonical
+// solution, 0 for a rotated copy.  `b(k)` reads board row k.
+template <typename B>
+__device__ __forceinline__ uint32_t classify(const B& b, int size, const UConf& c) {
+  int own, you;
+  uint32_t bit, ptn;
+  if (b(c.bound2) == 1u) {                        // 90 degrees
+    own = 1; ptn = 2;
+    while (own <= size - 1) {
+      bit = 1; you = size - 1;
+      while (b(you) != ptn && b(own) >= bit) { bit <<= 1; you--; }
+      if (b(own) > bit) return 0;
+      if (b(own) < bit) break;
+      own++; ptn <<= 1;
+    }
+    if (own > size - 1) return 2;
+  }
+  if (b(size - 1) == c.endbit) {                  // 180 degrees
+    own = 1; you = size - 2;
+    while (own <= size - 1) {
+      bit = 1; ptn = c.topbit;
+      while (b(you) != ptn && b(own) >= bit) { bit <<= 1; ptn >>= 1; }
+      if (b(own) > bit) return 0;
+      if (b(own) < bit) break;
+      own++; you--;
+    }
+    if (own > size - 1) return 4;
+  }
+  if (b(c.bound1) == c.topbit) {                  // 270 degrees
+    own = 1; ptn = c.topbit >> 1;
+    while (own <= size - 1) {
+      bit = 1; you = 0;
+      while (b(you) != ptn && b(own) >= bit) { bit <<= 1; you++; }
+      if (b(own) > bit) return 0;
+      if (b(own) < bit) break;
+      own++; ptn >>= 1;
+    }
+  }
+  return 8;
+}
+
+// Row rules of backTrack1/backTrack2 applied to the candidate set of `row`.
+__host__ __device__ __forceinline__ uint32_t row_filter(uint32_t bitmap, uint32_t row, uint32_t down, const UConf& c) {
+  if (c.part == 1) return row < c.bound1 ? (bitmap & ~2u) : bitmap;
+  if (row < c.bound1) return bitmap & ~c.sidemask;
+  if (row == c.bound2) {
+    const uint32_t ds = down & c.sidemask;
+    if (ds == 0u) return 0u;
+    if (ds != c.sidemask) return bitmap & c.sidemask;
+  }
+  return bitmap;
+}
+
+struct UArgs {
+  const UTask* tasks;
+  const UConf* confs;
+  int64_t m;
+  int N;
+  unsigned int* cursor;
+  unsigned long long* counts;   // c2, c4, c8
+  unsigned int* err;
+};
+
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK) unique_kernel(const UArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int N = a.N;
+  uint4* stk = reinterpret_cast<uint4*>(smem) + threadIdx.x;                            // N frames, stride BLOCK
+  uint32_t* brd = reinterpret_cast<uint32_t*>(smem + (size_t)N * BLOCK * sizeof(uint4)) + threadIdx.x;  // N rows
+  const unsigned lane = threadIdx.x & 31u;
+  const uint32_t mask = (N >= 32) ? FULLM : ((1u << N) - 1u);
+  uint32_t left = 0, down = 0, right = 0, avail = 0, row = 0, sp = 0;
+  UConf cf = {0, 0, 0, 0, 0, 0, 0};
+  unsigned long long c2 = 0, c4 = 0, c8 = 0;
+  bool exhausted = false;
+  for (;;) {
+    const bool idle = (avail | sp) == 0u;
+    if (__ballot_sync(FULLM, idle)) {
+      const bool want = idle && !exhausted;
+      const unsigned need = __ballot_sync(FULLM, want);
+      if (need) {
+        const int leader = __ffs(need) - 1;
+        unsigned base = 0;
+        if ((int)lane == leader) base = atomicAdd(a.cursor, (unsigned)__popc(need));
+        base = __shfl_sync(FULLM, base, leader);
+        if (want) {
+          const uint64_t slot = (uint64_t)base + (uint64_t)__popc(need & ((1u << lane) - 1u));
+          if (slot < (uint64_t)a.m) {
+            const UTask t = a.tasks[slot];
+            cf = a.confs[t.conf];
+            left = t.left; down = t.down; right = t.right; avail = t.avail; row = t.row; sp = 0;
+            for (uint32_t r = 0; r < t.row && r < (uint32_t)kBoardWords; r++) brd[r * BLOCK] = t.board[r];
+          } else {
+            exhausted = true;
+          }
+        }
+      }
+      if (__all_sync(FULLM, exhausted && (avail | sp) == 0u)) break;
+    }
+    if (avail == 0u && sp != 0u) {
+      --sp;
+      const uint4 f = stk[sp * BLOCK];
+      left = f.x; down = f.y; right = f.z; avail = f.w & 0x07FFFFFFu; row = f.w >> 27;
+    }
+    if (avail != 0u) {
+      const uint32_t bit = avail & (0u - avail);
+      avail -= bit;
+      brd[row * BLOCK] = bit;
+      const uint32_t nl = (left | bit) << 1, nd = down | bit, nr = (right | bit) >> 1;
+      const uint32_t nrow = row + 1;
+      uint32_t nb = mask & ~(nl | nd | nr);
+      if (nrow == (uint32_t)N - 1u) {                   // last row: a solution or none
+        if (cf.part == 1) {
+          if (nb) c8++;
+        } else if (nb && (nb & cf.lastmask) == 0u) {
+          brd[nrow * BLOCK] = nb;
+          const uint32_t k = classify([&](int r) { return brd[r * BLOCK]; }, N, cf);
+          c2 += (k == 2); c4 += (k == 4); c8 += (k == 8);
+        }
+      } else {
+        nb = row_filter(nb, nrow, nd, cf);
+        if (nb) {
+          if (avail) { stk[sp * BLOCK] = make_uint4(left, down, right, avail | (row << 27)); ++sp; }
+          left = nl; down = nd; right = nr; avail = nb; row = nrow;
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    c2 += __shfl_xor_sync(FULLM, c2, o);
+    c4 += __shfl_xor_sync(FULLM, c4, o);
+    c8 += __shfl_xor_sync(FULLM, c8, o);
+  }
+  if (lane == 0) {
+    if (c2) atomicAdd(a.counts + 0, c2);
+    if (c4) atomicAdd(a.counts + 1, c4);
+    if (c8) atomicAdd(a.counts + 2, c8);
+  }
+}
+
+// Host: every (part, bound1) start of 07Py_bit_symmetry.py NQueens() (:171-200),
+// expanded breadth-first over its first rows until there are enough tasks.
+int build_unique_tasks(int N, int64_t min_tasks, std::vector<UConf>& confs, std::vector<UTask>& tasks) {
+  const uint32_t mask = (1u << N) - 1u;
+  struct S { uint32_t left, down, right, row; uint32_t board[kBoardWords]; };
+  std::vector<std::pair<uint32_t, S>> cur;   // (conf, state at row with its candidate set still to take)
+  // part 1: corner queen
+  for (int b1 = 2; b1 < N - 1; b1++) {
+    UConf c = {1, (uint32_t)b1, 0, 0, 0, 0, 1u << (N - 1)};
+    confs.push_back(c);
+    const uint32_t bit = 1u << b1;
+    S s{};
+    s.left = (2u | bit) << 1; s.down = 1u | bit; s.right = (2u | bit) >> 1; s.row = 2;
+    s.board[0] = 1; s.board[1] = bit;
+    cur.push_back({(uint32_t)confs.size() - 1, s});
+  }
+  // part 2: no corner queen
+  {
+    const uint32_t topbit = 1u << (N - 1);
+    uint32_t endbit = topbit >> 1, lastmask = topbit | 1u;
+    const uint32_t sidemask = topbit | 1u;
+    for (int b1 = 1, b2 = N - 2; b1 > 0 && b2 < N - 1 && b1 < b2; b1++, b2--) {
+      UConf c = {2, (uint32_t)b1, (uint32_t)b2, endbit, lastmask, sidemask, topbit};
+      confs.push_back(c);
+      const uint32_t bit = 1u << b1;
+      S s{};
+      s.left = bit << 1; s.down = bit; s.right = bit >> 1; s.row = 1; s.board[0] = bit;
+      cur.push_back({(uint32_t)confs.size() - 1, s});
+      endbit >>= 1;
+      lastmask = (lastmask << 1) | lastmask | (lastmask >> 1);
+    }
+  }
+  // expand rows breadth-first while the tasks stay above the last row and fit the board prefix
+  std::vector<std::pair<uint32_t, S>> nxt;
+  while ((int64_t)cur.size() < min_tasks) {
+    bool grew = false;
+    nxt.clear();
+    for (auto& cs : cur) {
+      const UConf& c = confs[cs.first];
+      const S& s = cs.second;
+      if ((int)s.row + 1 >= N - 1 || s.row + 1 >= (uint32_t)kBoardWords) { nxt.push_back(cs); continue; }
+      uint32_t bm = row_filter(mask & ~(s.left | s.down | s.right), s.row, s.down, c);
+      while (bm) {
+        const uint32_t bit = bm & (0u - bm);
+        bm ^= bit;
+        S t = s;
+        t.board[s.row] = bit;
+        t.left = (s.left | bit) << 1; t.down = s.down | bit; t.right = (s.right | bit) >> 1; t.row = s.row + 1;
+        nxt.push_back({cs.first, t});
+        grew = true;
+      }
+    }
+    cur.swap(nxt);
+    if (!grew) break;
+  }
+  for (auto& cs : cur) {
+    const UConf& c = confs[cs.first];
+    const S& s = cs.second;
+    UTask t{};
+    t.left = s.left; t.down = s.down; t.right = s.right; t.row = s.row; t.conf = cs.first;
+    t.avail = row_filter(mask & ~(s.left | s.down | s.right), s.row, s.down, c);
+    for (int r = 0; r < kBoardWords; r++) t.board[r] = s.board[r];
+    if (t.avail) tasks.push_back(t);
+  }
+  return 0;
+}
+
+}  // namespace
+}  // namespace nq
+
+using namespace nq;
+
+extern "C" int nq_count_unique(nq_handle* h, int N, uint64_t* unique, uint64_t* total) {
+  if (!h || !unique || !total) return NQ_EINVAL;
+  if (N < 4 || N > kMaxN) return NQ_EINVAL;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return NQ_ECUDA;
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  std::vector<UConf> confs;
+  std::vector<UTask> tasks;
+  build_unique_tasks(N, (int64_t)sms * 2048 * 8, confs, tasks);
+  const int64_t m = (int64_t)tasks.size();
+  constexpr int B = 128;
+  const size_t smem = (size_t)B * N * (sizeof(uint4) + sizeof(uint32_t));
+  void *d_tasks = nullptr, *d_confs = nullptr, *d_ctl = nullptr;
+  cudaStream_t st = nullptr;
+  int status = NQ_OK;
+  unsigned long long hc[3] = {0, 0, 0};
+  uint32_t herr = 0;
+  do {
+    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) { status = NQ_ECUDA; break; }
+    if (cudaMallocAsync(&d_tasks, std::max<size_t>(1, (size_t)m * sizeof(UTask)), st) != cudaSuccess ||
+        cudaMallocAsync(&d_confs, std::max<size_t>(1, confs.size() * sizeof(UConf)), st) != cudaSuccess ||
+        cudaMallocAsync(&d_ctl, 64, st) != cudaSuccess) { status = NQ_ENOMEM; break; }
+    if (cudaMemsetAsync(d_ctl, 0, 64, st) != cudaSuccess) { status = NQ_ECUDA; break; }
+    if (m > 0 && cudaMemcpyAsync(d_tasks, tasks.data(), (size_t)m * sizeof(UTask), cudaMemcpyHostToDevice, st) != cudaSuccess) { status = NQ_ECUDA; break; }
+    if (!confs.empty() && cudaMemcpyAsync(d_confs, confs.data(), confs.size() * sizeof(UConf), cudaMemcpyHostToDevice, st) != cudaSuccess) { status = NQ_ECUDA; break; }
+    if (m > 0) {
+      if (cudaFuncSetAttribute(unique_kernel<B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) { status = NQ_ECUDA; break; }
+      int per = 0;
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, unique_kernel<B>, B, smem) != cudaSuccess || per <= 0) { status = NQ_ECUDA; break; }
+      UArgs a;
+      a.tasks = (const UTask*)d_tasks; a.confs = (const UConf*)d_confs; a.m = m; a.N = N;
+      a.counts = (unsigned long long*)d_ctl; a.cursor = (unsigned int*)((char*)d_ctl + 32);
+      a.err = (unsigned int*)((char*)d_ctl + 36);
+      unique_kernel<B><<<sms * per, B, smem, st>>>(a);
+      if (cudaGetLastError() != cudaSuccess) { status = NQ_ECUDA; break; }
+    }
+    if (cudaMemcpyAsync(hc, d_ctl, 24, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaMemcpyAsync(&herr, (char*)d_ctl + 36, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess) { status = NQ_ECUDA; break; }
+  } while (0);
+  if (st) {
+    if (d_tasks) cudaFreeAsync(d_tasks, st);
+    if (d_confs) cudaFreeAsync(d_confs, st);
+    if (d_ctl) cudaFreeAsync(d_ctl, st);
+    cudaStreamSynchronize(st);
+    cudaStreamDestroy(st);
+  }
+  if (status != NQ_OK) return status;
+  if (herr) return NQ_EINVAL;
+  *unique = hc[0] + hc[1] + hc[2];
+  *total = 2 * hc[0] + 4 * hc[1] + 8 * hc[2];
+  return NQ_OK;
+}

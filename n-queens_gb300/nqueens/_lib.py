@@ -74,6 +74,7 @@ SIGNATURES = {
     "nq_last_run_info": (ctypes.c_int, [_vp, _ip, ctypes.POINTER(ctypes.c_int64)]),
     "nq_last_kernel_ms": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
     "nq_count": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _u64p]),
+    "nq_count_unique": (ctypes.c_int, [_vp, ctypes.c_int, _u64p, _u64p]),
     "nq_count_completions": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _ip, _ip, _u64p]),
     "nq_debug_task_schedule": (ctypes.c_int, [ctypes.c_int, nq_record, _u32p, _u32p, _u32p, ctypes.c_int]),
     "nq_debug_completion_tasks": (ctypes.c_int64, [ctypes.c_int, ctypes.c_int, _ip, _ip, ctypes.c_int, _u32p,

@@ -111,7 +111,8 @@ def records_from_constellations(constellations: Sequence[Dict[str, int]]) -> np.
 
 @dataclass
 class Result:
-    """Board totals (unique is 0 on the constellation path, as the reference prints)."""
+    """Board totals.  ``unique`` is 0 on the constellation path, as the reference prints;
+    ``Engine.count_unique`` fills it with the symmetry method."""
     total: int
     unique: int = 0
 
@@ -270,6 +271,13 @@ class Engine:
         _check(lib().nq_count(self._h, int(N), int(preset or 0), _lib.p64(t)), self._h, f"count(N={N})")
         return Result(total=int(t[0]))
 
+    def count_unique(self, N: int) -> Result:
+        """Unique and total counts by the symmetry method (07Py_bit_symmetry.py), 4 <= N <= 27."""
+        u = np.zeros(1, np.uint64)
+        t = np.zeros(1, np.uint64)
+        _check(lib().nq_count_unique(self._h, int(N), _lib.p64(u), _lib.p64(t)), self._h, f"count_unique(N={N})")
+        return Result(total=int(t[0]), unique=int(u[0]))
+
     def count_completions(self, N: int, queens: Sequence[Tuple[int, int]]) -> int:
         """Number of full placements containing the pre-placed (row, col) queens."""
         q = list(queens)
@@ -342,6 +350,9 @@ def exec_solutions(N: int, constellations: List[Dict[str, int]], use_gpu: bool =
         print(f"[gpu-summary] N={N} constellations={len(constellations)} total={total}")
 
 
-def count(N: int, preset: Optional[int] = None) -> Result:
-    """Whole-board total for N on the default engine (device 0)."""
+def count(N: int, preset: Optional[int] = None, unique: bool = False) -> Result:
+    """Whole-board total for N on the default engine (device 0).  With unique=True
+    both counts come from the symmetry method (N >= 4)."""
+    if unique:
+        return default_engine().count_unique(N)
     return default_engine().count(N, preset)
