@@ -427,7 +427,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--block", type=int, default=128)
+    ap.add_argument("--block", type=int, default=64)
     ap.add_argument("--split", type=int, default=-1, help="split depth (-1 automatic)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")

@@ -47,6 +47,8 @@ const char *nq_strerror(int status);
 int nq_create(nq_handle **out, int device);
 void nq_destroy(nq_handle *h);
 int nq_last_error(const nq_handle *h, char *buf, size_t cap);
+/* Name of the handle's GPU (the key of the autotuner's tables). */
+int nq_device_name(const nq_handle *h, char *buf, size_t cap);
 
 /* Launch knobs chosen by the autotuner: threads per block (64, 128 or 256),
  * grid (0 = one wave of resident blocks) and split depth (-1 = automatic,

@@ -76,12 +76,16 @@ const char* derr_text(uint32_t e) {
   return "ok";
 }
 
-// Expand tasks until the queue holds about 24 subtasks per resident lane
-// (each level multiplies the task count by roughly 4), at most 3 levels.
-int choose_split(int64_t m, int64_t lanes) {
+// Expand tasks until the queue holds at least 13 items per resident DFS lane
+// (the DFS kernel keeps about 768 lanes per SM), at most 3 levels.  Each level
+// multiplies the queue by about 7 (measured: 6.2x at N=16 to 8x at N=20);
+// this rule picks the depth the autotuner found fastest on GB300 for N=16..20
+// (2, 2, 1, 1, 1).
+int choose_split(int64_t m, int sms) {
+  const double target = 13.0 * 768.0 * (double)sms;
   int D = 0;
   double est = (double)m;
-  while (D < 3 && est < 24.0 * (double)lanes) { est *= 4.0; D++; }
+  while (D < 3 && est < target) { est *= 7.0; D++; }
   return D;
 }
 
@@ -98,7 +102,7 @@ struct nq_handle {
   int device = 0;
   int sms = 0;
   cudaStream_t stream = nullptr;
-  int block = 128, grid = 0, split = -1;   // split: -1 automatic, 0..3 fixed depth
+  int block = 64, grid = 0, split = -1;    // split: -1 automatic, 0..3 fixed depth
   std::string err;
   DevBuf rec, root, info, sched, per_task, ctrl, nsub, sroot, sinfo;
   uint64_t* h_ctrl = nullptr;   // pinned read-back of the control block
@@ -166,11 +170,6 @@ struct nq_handle {
 
 namespace {
 
-int64_t resident_lanes(nq_handle* h, bool wide, int maxt) {
-  const int per = dfs_blocks_per_sm(wide, h->block, maxt);
-  const int64_t grid = h->grid > 0 ? h->grid : (int64_t)h->sms * std::max(1, per);
-  return grid * h->block;
-}
 
 // records (device) -> counts on st; totals land in ctrl[0].  Launches
 // prepare, then (when splitting) the split count pass, one 8-byte read-back
@@ -194,7 +193,7 @@ int run_records(nq_handle* h, int N, const uint4* d_rec, int64_t m, int start_mi
   unsigned long long* sctr = (unsigned long long*)(c + 16);   // split: [0] subtasks, [1] allocation cursor
   NQ_CUDA(h, cudaEventRecord(h->ev[0], st));
   NQ_CUDA(h, launch_prepare(N, m, d_rec, ta, 0, 0, err, st));
-  const int D = h->split >= 0 ? h->split : choose_split(m, resident_lanes(h, false, maxt));
+  const int D = h->split >= 0 ? h->split : choose_split(m, h->sms);
   DfsLaunch L;
   L.tasks = ta; L.m = m; L.order = nullptr; L.cursor = cursor; L.job_totals = totals;
   L.per_task = d_per_task; L.err = err; L.maxt = maxt; L.block = h->block; L.grid = h->grid; L.big = N >= 24;
@@ -323,6 +322,14 @@ int nq_last_kernel_ms(nq_handle* h, float* prepare_ms, float* dfs_ms) {
   NQ_CUDA(h, cudaEventElapsedTime(&b, h->ev[1], h->ev[2]));
   if (prepare_ms) *prepare_ms = a;
   if (dfs_ms) *dfs_ms = b;
+  return NQ_OK;
+}
+
+int nq_device_name(const nq_handle* h, char* buf, size_t cap) {
+  if (!h || !buf || cap == 0) return NQ_EINVAL;
+  cudaDeviceProp p;
+  if (cudaGetDeviceProperties(&p, h->device) != cudaSuccess) return NQ_ECUDA;
+  snprintf(buf, cap, "%s", p.name);
   return NQ_OK;
 }
 
@@ -704,8 +711,7 @@ int nq_batch_create(nq_handle* h, const nq_job* jobs, int njobs, nq_batch** out)
     unsigned long long* sc = (unsigned long long*)sctr.p;   // [2j] subtasks of job j, [2*njobs+1] cursor
     if ((e = cudaMemsetAsync(sc, 0, (size_t)(njobs + 1) * 16, st)) != cudaSuccess) { sctr.release(); break; }
     for (int j = 0; j < njobs && e == cudaSuccess; j++) {
-      const int64_t lanes = resident_lanes(h, b->wide, b->job_maxt[j]);
-      b->job_split[j] = (jobs[j].N <= 12) ? 0 : (h->split >= 0 ? h->split : choose_split(b->job_m[j], lanes));
+      b->job_split[j] = (jobs[j].N <= 12) ? 0 : (h->split >= 0 ? h->split : choose_split(b->job_m[j], h->sms));
       e = launch_split(0, b->job_split[j], b->job_off[j], b->job_m[j], ta, (uint32_t*)b->nsub.p, nullptr, nullptr,
                        sc + 2 * j, nullptr, nullptr, 0, st);
     }

@@ -60,6 +60,7 @@ SIGNATURES = {
     "nq_create": (ctypes.c_int, [ctypes.POINTER(_vp), ctypes.c_int]),
     "nq_destroy": (None, [_vp]),
     "nq_last_error": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_size_t]),
+    "nq_device_name": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_size_t]),
     "nq_set_config": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "nq_get_config": (ctypes.c_int, [_vp, _ip, _ip, _ip]),
     "nq_preset_for": (ctypes.c_int, [ctypes.c_int]),

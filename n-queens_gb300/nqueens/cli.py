@@ -37,11 +37,11 @@ def main(argv=None) -> int:
     ap.add_argument("nmax", nargs="?", type=int, default=20, help="exclusive upper bound, as range()")
     ap.add_argument("--repeat", type=int, default=1)
     ap.add_argument("--split", type=int, default=-1)
-    ap.add_argument("--block", type=int, default=128)
+    ap.add_argument("--block", type=int, default=64)
     ap.add_argument("--device", type=int, default=0)
     ap.add_argument("--unique", action="store_true", help="also count unique solutions (symmetry method)")
     a = ap.parse_args(argv)
-    eng = Engine(a.device, block=a.block, split=a.split)
+    eng = Engine(a.device, block=a.block, split=a.split)   # the defaults keep the autotuned table
     print(" N:             Total           Unique         hh:mm:ss.ms")
     rc = 0
     for N in range(a.nmin, a.nmax):

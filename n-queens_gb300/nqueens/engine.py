@@ -207,18 +207,36 @@ class Batch:
 class Engine:
     """One CUDA device and stream of libnqgpu.so."""
 
-    def __init__(self, device: int = 0, block: int = 128, grid: int = 0, split: int = -1):
+    def __init__(self, device: int = 0, block: int = 64, grid: int = 0, split: int = -1, auto_tune: bool = True):
+        """auto_tune: when nqueens/tuning.json holds a table for this GPU, each count of an N in
+        the table uses its tuned block, grid and split depth (explicit set_config turns this off)."""
         h = ctypes.c_void_p()
         _check(lib().nq_create(ctypes.byref(h), int(device)), what=f"nq_create(device={device})")
         self._h = h
         self.device = device
+        self._tuning = None
         self.set_config(block, grid, split)
+        if auto_tune and (block, grid, split) == (64, 0, -1):
+            from . import tune
+            self._tuning = tune.load(self.device_name())
+
+    def device_name(self) -> str:
+        buf = ctypes.create_string_buffer(256)
+        _check(lib().nq_device_name(self._h, buf, 256), self._h, "device_name")
+        return buf.value.decode()
+
+    def _apply_tuning(self, N: int) -> None:
+        if self._tuning and str(N) in self._tuning:
+            t = self._tuning[str(N)]
+            _check(lib().nq_set_config(self._h, int(t["block"]), int(t["grid"]), int(t["split"])), self._h)
 
     # -- configuration ---------------------------------------------------
-    def set_config(self, block: int = 128, grid: int = 0, split: int = -1) -> None:
+    def set_config(self, block: int = 64, grid: int = 0, split: int = -1) -> None:
         """Threads per block (64/128/256), grid (0: one wave of resident blocks) and split depth
-        (-1: automatic, 0..3: expand every task that many levels before the DFS)."""
+        (-1: automatic, 0..3: expand every task that many levels before the DFS).  Turns the
+        autotuned per-N configuration off."""
         _check(lib().nq_set_config(self._h, block, grid, split), self._h, "set_config")
+        self._tuning = None
 
     def get_config(self) -> Tuple[int, int, int]:
         b, g, o = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
@@ -230,6 +248,7 @@ class Engine:
         """Count host records; returns (total, per-record weighted counts or None)."""
         rec = np.ascontiguousarray(records, RECORD_DTYPE)
         m = int(rec.shape[0])
+        self._apply_tuning(N)
         total = np.zeros(1, np.uint64)
         sol = np.zeros(m, np.uint64) if want_solutions else None
         _check(lib().nq_exec_solutions(self._h, int(N), rec.ctypes.data_as(ctypes.c_void_p), m,
@@ -268,6 +287,7 @@ class Engine:
     def count(self, N: int, preset: Optional[int] = None) -> Result:
         """Whole-board total (constellation path for N >= 6, GPU brute force for N <= 5)."""
         t = np.zeros(1, np.uint64)
+        self._apply_tuning(N)
         _check(lib().nq_count(self._h, int(N), int(preset or 0), _lib.p64(t)), self._h, f"count(N={N})")
         return Result(total=int(t[0]))
 
@@ -325,7 +345,7 @@ def default_engine() -> Engine:
     return _default
 
 
-def exec_solutions(N: int, constellations: List[Dict[str, int]], use_gpu: bool = True, gpu_block: int = 128,
+def exec_solutions(N: int, constellations: List[Dict[str, int]], use_gpu: bool = True, gpu_block: int = 64,
                    gpu_max_blocks: int = 0, gpu_log_level: int = 0, gpu_sort_mode: int = -1, **_ignored) -> None:
     """Drop-in for exec_solutions (356Py:2228-2610), GPU branch.
 
@@ -341,7 +361,7 @@ def exec_solutions(N: int, constellations: List[Dict[str, int]], use_gpu: bool =
         return
     eng = default_engine()
     _, _, split = eng.get_config()
-    eng.set_config(gpu_block if gpu_block in (64, 128, 256) else 128, max(0, int(gpu_max_blocks)), split)
+    eng.set_config(gpu_block if gpu_block in (64, 128, 256) else 64, max(0, int(gpu_max_blocks)), split)
     recs = records_from_constellations(constellations)
     total, sol = eng.exec_records(N, recs, want_solutions=True)
     for c, v in zip(constellations, sol.tolist()):
