@@ -1,0 +1,74 @@
+"""Chunked counting with a progress file, so a long count can resume.
+
+The reference's restart unit is the chunk (``chunk_only`` / ``debug_chunk_start``
+/ ``chunk_list_spec``, 14Bit_codon_GPU/356Py_savesp_narrow.py:2418-2435 and
+:5539-5550) with a per-chunk progress TSV (:3330-3338).  Here the task list is
+cut into fixed chunks; after each chunk one line ``chunk<TAB>first<TAB>end<TAB>total``
+is appended to the progress file and flushed, and a rerun skips the chunks
+already recorded.  The file starts with a header naming N, the record count and
+a digest of the records, so a progress file never resumes a different task list.
+"""
+from __future__ import annotations
+
+import hashlib
+import os
+from typing import Callable, Dict, Optional
+
+import numpy as np
+
+from ._lib import RECORD_DTYPE
+
+
+def _digest(records: np.ndarray) -> str:
+    return hashlib.sha256(np.ascontiguousarray(records, RECORD_DTYPE).tobytes()).hexdigest()[:32]
+
+
+def _header(N: int, records: np.ndarray, chunk: int) -> str:
+    return f"# nqueens progress N={N} records={len(records)} chunk={chunk} sha256={_digest(records)}\n"
+
+
+def read_progress(path: str, header: str) -> Dict[int, int]:
+    """Chunk index -> total from a progress file written for the same task list."""
+    if not os.path.exists(path):
+        return {}
+    done: Dict[int, int] = {}
+    with open(path) as f:
+        first = f.readline()
+        if first != header:
+            raise ValueError(f"{path} belongs to another task list or chunk size")
+        for line in f:
+            parts = line.rstrip("\n").split("\t")
+            if len(parts) != 4:
+                break                      # a torn last line from an interrupted write: redo that chunk
+            done[int(parts[0])] = int(parts[3])
+    return done
+
+
+def exec_records_resumable(counter: Callable[[int, np.ndarray], int], N: int, records: np.ndarray,
+                           progress_path: str, chunk: int = 1 << 20,
+                           stop_after: Optional[int] = None) -> Optional[int]:
+    """Total over all chunks, resuming from progress_path.  ``counter(N, recs) -> total``
+    counts one chunk (an Engine's exec_records, for instance).  ``stop_after`` returns None
+    after that many newly counted chunks (an interruption, for tests)."""
+    rec = np.ascontiguousarray(records, RECORD_DTYPE)
+    header = _header(N, rec, chunk)
+    done = read_progress(progress_path, header)
+    if not os.path.exists(progress_path):
+        with open(progress_path, "w") as f:
+            f.write(header)
+    n_chunks = (len(rec) + chunk - 1) // chunk
+    counted = 0
+    with open(progress_path, "a") as f:
+        for c in range(n_chunks):
+            if c in done:
+                continue
+            if stop_after is not None and counted >= stop_after:
+                return None
+            a, b = c * chunk, min(len(rec), (c + 1) * chunk)
+            t = int(counter(N, rec[a:b]))
+            f.write(f"{c}\t{a}\t{b}\t{t}\n")
+            f.flush()
+            os.fsync(f.fileno())
+            done[c] = t
+            counted += 1
+    return sum(done[c] for c in range(n_chunks))

@@ -220,3 +220,34 @@ def test_batch_mixed_jobs(eng, oracle_mod):
         assert out is not None and np.array_equal(out, want)
     finally:
         b.close()
+
+
+def test_stack_shorter_than_a_task_is_an_error_not_a_partial_count(eng):
+    """A start row claimed too deep sizes the stack too small: the call fails with NQ_ESTACK."""
+    torch = pytest.importorskip("torch")
+    import nqueens
+    N = 12
+    recs = nqueens.gen_records(N)
+    d_rec = torch.from_numpy(recs.view(np.uint8).copy()).cuda()
+    d_total = torch.zeros(1, dtype=torch.int64, device="cuda")
+    eng.set_config(64, 0, 0)
+    try:
+        eng.exec_device(N, d_rec.data_ptr(), len(recs), 9, d_total.data_ptr())   # real start rows are 2..4
+        with pytest.raises(nqueens.NQError) as ei:
+            eng.sync()
+        assert ei.value.status == -2
+        eng.exec_device(N, d_rec.data_ptr(), len(recs), int((recs["startijkl"] >> 20).min()), d_total.data_ptr())
+        eng.sync()
+        assert int(d_total.item()) == 14200                   # the handle stays usable
+    finally:
+        eng.set_config(64, 0, -1)
+
+
+def test_resumable_count_on_gpu(eng, oracle_mod, tmp_path):
+    import nqueens
+    from nqueens.checkpoint import exec_records_resumable
+    recs = nqueens.gen_records(17)
+    p = str(tmp_path / "p.tsv")
+    counter = lambda n, r: eng.exec_records(n, r)[0]
+    assert exec_records_resumable(counter, 17, recs, p, chunk=8192, stop_after=2) is None
+    assert exec_records_resumable(counter, 17, recs, p, chunk=8192) == oracle_mod.EXPECTED_TOTAL[17]
