@@ -216,6 +216,11 @@ NQ_HD int walk_schedule(int N, const TaskHead& t, Root* root, uint32_t* root_cou
       }
       ops[d - 1].term = 1;
       ops[d - 1].b14 = (fid == 14);
+      // The terminal-parent frame never descends, so its LA bits only feed the
+      // child row's free set: LA bit 0 there removes column 0, which is the
+      // SQd2B base rule "count only if a square other than column 0 is free"
+      // (356Py:1855-1860).
+      if (fid == 14) ops[d - 1].la |= 1u;
       return d - 1;
     }
     if (d >= max_depth || row > 31) return -2;

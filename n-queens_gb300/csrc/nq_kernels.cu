@@ -283,14 +283,15 @@ struct Lane {
     const uint32_t nld = ((ld + bit) << o.s) | o.la;
     const uint32_t nrd = ((rd + bit) >> o.s) | o.ra;
     const uint32_t ncol = col + bit;
-    uint32_t nf = bm & ~(nld | nrd | ncol);
+    const uint32_t nf = bm & ~(nld | nrd | ncol);
     const uint32_t ahead = bm & ~((nld + nld) | (nrd >> 1) | ncol);
-    if (ahead == 0u && o.fc) nf = 0;
-    const uint32_t tm = o.term ? (o.b14 ? ~1u : ~0u) : 0u;   // terminal: count instead of descend
-    bool hit = (nf & tm) != 0u;
-    if constexpr (WIDE) hit = hit || (o.term && o.tall);
-    cnt += (act && hit) ? 1u : 0u;
-    const bool desc = act && tm == 0u && nf != 0u;
+    // terminal depth: count the child (the SQd2B rule is LA bit 0 of the word);
+    // otherwise descend unless the child row or, with look-ahead, the row after is full
+    const bool live = act && nf != 0u;
+    bool hit = live && o.term;
+    if constexpr (WIDE) hit = hit || (act && o.term && o.tall);
+    cnt += hit ? 1u : 0u;
+    const bool desc = live && !o.term && !(o.fc && ahead == 0u);
     if (desc && avail != 0u) { stk[sp * BLOCK] = make_uint4(ld, rd, col, avail | (d << 27)); ++sp; }
     if (desc) { ld = nld; rd = nrd; col = ncol; avail = nf; ++d; }
   }
