@@ -10,7 +10,7 @@
 //   kernel_dfs_iter_gpu_maxd14..21 (356Py:618-1747) and dfs_iter
 //   (356Py:1837-1967).  Every lane runs its own task; a lane whose task is
 //   done takes the next one from a global queue (one atomicAdd per warp and
-//   refill round, ranks by ballot).  Each loop iteration every busy lane
+//   refill round, ranks by ballot).  Each step every busy lane
 //   expands exactly one candidate queen, so lanes stay converged on the same
 //   short instruction sequence whatever their task, depth or SQ* variant:
 //   the variant lives in the schedule word read from shared memory, not in
@@ -27,6 +27,19 @@
 namespace nq {
 
 constexpr unsigned FULL = 0xFFFFFFFFu;
+
+// DFS steps each lane takes between two checks for finished lanes (flush +
+// refill).  A lane that runs dry mid-round idles for the rest of the round; a
+// check costs two ballots, so checking less often wins until that idle time
+// dominates.
+#ifndef NQ_STEPS_PER_CHECK
+#define NQ_STEPS_PER_CHECK 32
+#endif
+#ifndef NQ_STEP_UNROLL
+#define NQ_STEP_UNROLL 16
+#endif
+constexpr int kStepsPerCheck = NQ_STEPS_PER_CHECK;
+constexpr int kStepUnroll = NQ_STEP_UNROLL;
 
 template <bool WIDE> struct WordT { using type = uint32_t; };
 template <> struct WordT<true> { using type = uint2; };
@@ -267,11 +280,12 @@ struct Lane {
   uint32_t ld = 0, rd = 0, col = 0, avail = 0, bm = 0, d = 0, sp = 0;
   typename std::conditional<BIG, unsigned long long, uint32_t>::type cnt = 0;
 
+  // sp is the byte offset of the next free frame in this lane's interleaved stack
   template <int BLOCK>
-  __device__ __forceinline__ void step(uint4* stk, const typename WordT<WIDE>::type* sch) {
+  __device__ __forceinline__ void step(unsigned char* stk, const typename WordT<WIDE>::type* sch) {
     if (avail == 0 && sp != 0) {
-      --sp;
-      const uint4 f = stk[sp * BLOCK];
+      sp -= BLOCK * (uint32_t)sizeof(uint4);
+      const uint4 f = *reinterpret_cast<const uint4*>(stk + sp);
       ld = f.x; rd = f.y; col = f.z;
       avail = f.w & 0x07FFFFFFu;
       d = f.w >> 27;
@@ -292,7 +306,10 @@ struct Lane {
     if constexpr (WIDE) hit = hit || (act && o.term && o.tall);
     cnt += hit ? 1u : 0u;
     const bool desc = live && !o.term && !(o.fc && ahead == 0u);
-    if (desc && avail != 0u) { stk[sp * BLOCK] = make_uint4(ld, rd, col, avail | (d << 27)); ++sp; }
+    if (desc && avail != 0u) {
+      *reinterpret_cast<uint4*>(stk + sp) = make_uint4(ld, rd, col, avail | (d << 27));
+      sp += BLOCK * (uint32_t)sizeof(uint4);
+    }
     if (desc) { ld = nld; rd = nrd; col = ncol; avail = nf; ++d; }
   }
 };
@@ -306,6 +323,7 @@ __global__ void __launch_bounds__(BLOCK) dfs_kernel(const DfsArgs a) {
   const unsigned lane = threadIdx.x & 31u;
   const unsigned lt_mask = (1u << lane) - 1u;
   const W* __restrict__ gsched = reinterpret_cast<const W*>(a.sched);
+  unsigned char* stkb = reinterpret_cast<unsigned char*>(stk);   // this lane's stack, byte-addressed
   Lane<WIDE, BIG> L;
   uint32_t wexp = 0, job = a.job_base, task = 0;
   bool have = false, exhausted = false;
@@ -365,8 +383,8 @@ __global__ void __launch_bounds__(BLOCK) dfs_kernel(const DfsArgs a) {
       }
       if (__all_sync(FULL, exhausted && (L.avail | L.sp) == 0u)) break;
     }
-    L.template step<BLOCK>(stk, sch);
-    L.template step<BLOCK>(stk, sch);
+#pragma unroll kStepUnroll
+    for (int s = 0; s < kStepsPerCheck; ++s) L.template step<BLOCK>(stkb, sch);
   }
 
   const uint32_t j0 = __shfl_sync(FULL, acc_job, 0);
