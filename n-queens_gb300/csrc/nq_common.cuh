@@ -37,7 +37,7 @@
 
 namespace nq {
 
-constexpr int kMaxN = 27;        // avail | depth<<27 packing and u64 totals
+constexpr int kMaxN = 27;        // columns in bits 0-26, a frame's depth in bits 27-31; u64 totals
 constexpr int kMaxDepth = 28;    // schedule words per task (depths 0..T)
 
 // compact word fields

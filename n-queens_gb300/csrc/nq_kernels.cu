@@ -275,9 +275,13 @@ size_t dfs_smem_bytes(bool wide, int block, int maxt) {
 // '|' where the bits are disjoint (a candidate is never in ld, rd or col),
 // so those adds issue on the FMA pipe as well as the ALU pipe.  Per-task
 // counts are u32 (BIG: u64, for N >= 24, where one task may pass 2^32).
+static_assert(kMaxN <= 27, "a frame's depth is kept in col bits 27-31");
+
 template <bool WIDE, bool BIG>
 struct Lane {
-  uint32_t ld = 0, rd = 0, col = 0, avail = 0, bm = 0, d = 0, sp = 0;
+  // col bits 27-31 hold the depth of the frame (bm masks them out of every use
+  // of col as a column set), so a saved frame is exactly {ld, rd, col, avail}
+  uint32_t ld = 0, rd = 0, col = 0, avail = 0, bm = 0, sp = 0;
   typename std::conditional<BIG, unsigned long long, uint32_t>::type cnt = 0;
 
   // sp is the byte offset of the next free frame in this lane's interleaved stack
@@ -286,10 +290,9 @@ struct Lane {
     if (avail == 0 && sp != 0) {
       sp -= BLOCK * (uint32_t)sizeof(uint4);
       const uint4 f = *reinterpret_cast<const uint4*>(stk + sp);
-      ld = f.x; rd = f.y; col = f.z;
-      avail = f.w & 0x07FFFFFFu;
-      d = f.w >> 27;
+      ld = f.x; rd = f.y; col = f.z; avail = f.w;
     }
+    const uint32_t d = col >> 27;
     const bool act = avail != 0;
     const uint32_t bit = avail & (0u - avail);
     avail -= bit;
@@ -297,8 +300,9 @@ struct Lane {
     const uint32_t nld = ((ld + bit) << o.s) | o.la;
     const uint32_t nrd = ((rd + bit) >> o.s) | o.ra;
     const uint32_t ncol = col + bit;
-    const uint32_t nf = bm & ~(nld | nrd | ncol);
-    const uint32_t ahead = bm & ~((nld + nld) | (nrd >> 1) | ncol);
+    const uint32_t free_cols = bm & ~ncol;
+    const uint32_t nf = free_cols & ~(nld | nrd);
+    const uint32_t ahead = free_cols & ~((nld + nld) | (nrd >> 1));
     // terminal depth: count the child (the SQd2B rule is LA bit 0 of the word);
     // otherwise descend unless the child row or, with look-ahead, the row after is full
     const bool live = act && nf != 0u;
@@ -307,10 +311,10 @@ struct Lane {
     cnt += hit ? 1u : 0u;
     const bool desc = live && !o.term && !(o.fc && ahead == 0u);
     if (desc && avail != 0u) {
-      *reinterpret_cast<uint4*>(stk + sp) = make_uint4(ld, rd, col, avail | (d << 27));
+      *reinterpret_cast<uint4*>(stk + sp) = make_uint4(ld, rd, col, avail);
       sp += BLOCK * (uint32_t)sizeof(uint4);
     }
-    if (desc) { ld = nld; rd = nrd; col = ncol; avail = nf; ++d; }
+    if (desc) { ld = nld; rd = nrd; col = ncol + (1u << 27); avail = nf; }
   }
 };
 
@@ -365,14 +369,14 @@ __global__ void __launch_bounds__(BLOCK) dfs_kernel(const DfsArgs a) {
             wexp = info_wexp(in.x);
             job = in.y;
             L.bm = (1u << info_N(in.x)) - 1u;
-            L.d = 0; L.sp = 0;
+            L.sp = 0;
             if (T == INFO_NO_DFS || info_status(in.x) != TS_OK || T < d0) {
               L.avail = 0;
             } else if ((int)(T - d0) > a.maxt) {    // frames at depths 0..T'-1, words 0..T'
               atomicOr(a.err, DERR_DEPTH);
               L.avail = 0;
             } else {
-              L.ld = r.x; L.rd = r.y; L.col = r.z; L.avail = r.w;
+              L.ld = r.x; L.rd = r.y; L.col = r.z & L.bm; L.avail = r.w;
               const W* src = gsched + (size_t)task * a.sw + d0;
               for (uint32_t k = 0; k <= T - d0; k++) sch[k * BLOCK] = src[k];
             }
