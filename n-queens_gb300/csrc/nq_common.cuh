@@ -192,6 +192,20 @@ NQ_HD TaskHead decode_record(int N, uint32_t rld, uint32_t rrd, uint32_t rcol, u
 // One schedule entry before packing.
 struct Op { uint32_t s, la, ra, fc, term, b14, tall; };
 
+// Look-ahead wherever it is sound, not only where the reference applies it
+// (fr.av == 1 frames).  A word's look-ahead prunes the child frame when the
+// row after the child has no square free of the child's ld << 1, rd >> 1 and
+// col.  If the child's own step is a single row (s == 1) that set contains
+// every grandchild's free set, whatever square the child takes and whatever
+// the child's word adds through la/ra, so an empty set means every child
+// candidate dies (or, at a terminal parent, counts nothing): pruning there
+// changes no count.  A tall terminal counts its candidates without looking
+// at a further row, so a child with a tall word is never pruned.
+NQ_HD void extend_lookahead(Op* ops, int T) {
+  for (int d = 0; d < T; d++)
+    if (ops[d + 1].s == 1 && !ops[d + 1].tall) ops[d].fc = 1;
+}
+
 // Walk the SQ* state machine from the task's root frame and emit one Op per
 // depth 0..T (dfs_iter, 356Py:1846-1965, with rows advancing by the op's
 // step).  Root adjustments (the root frame's own jmark, 356Py:1889-1897, or
@@ -221,6 +235,7 @@ NQ_HD int walk_schedule(int N, const TaskHead& t, Root* root, uint32_t* root_cou
       // SQd2B base rule "count only if a square other than column 0 is free"
       // (356Py:1855-1860).
       if (fid == 14) ops[d - 1].la |= 1u;
+      extend_lookahead(ops, d - 1);
       return d - 1;
     }
     if (d >= max_depth || row > 31) return -2;

@@ -251,6 +251,7 @@ int build_completion_tasks(int N, int k, const int* rows, const int* cols, int m
   for (int d = 0; d + 1 < n; d++) ops[d].s = (uint32_t)(F[d + 1] - F[d]);
   ops[n - 1].term = 1; ops[n - 1].tall = 1;
   const int T = n - 1;
+  extend_lookahead(ops, T);
   for (int d = 0; d < n; d++)
     if (ops[d].s > 7 || (ops[d].la & ~W_LA)) return -1;
 
