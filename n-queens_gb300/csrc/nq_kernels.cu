@@ -277,26 +277,42 @@ size_t dfs_smem_bytes(bool wide, int block, int maxt) {
 // counts are u32 (BIG: u64, for N >= 24, where one task may pass 2^32).
 static_assert(kMaxN <= 27, "a frame's depth is kept in col bits 27-31");
 
+// Shared-memory accesses of the step, as predicated PTX so the pop and the push
+// are single predicated instructions rather than branches around them.
+// Addresses are 32-bit shared-window addresses.
+__device__ __forceinline__ uint32_t lds_word(uint32_t a, uint32_t) {
+  uint32_t w;
+  asm volatile("ld.shared.u32 %0, [%1];" : "=r"(w) : "r"(a));
+  return w;
+}
+__device__ __forceinline__ uint2 lds_word(uint32_t a, uint2) {
+  uint2 w;
+  asm volatile("ld.shared.v2.u32 {%0, %1}, [%2];" : "=r"(w.x), "=r"(w.y) : "r"(a));
+  return w;
+}
+
 template <bool WIDE, bool BIG>
 struct Lane {
   // col bits 27-31 hold the depth of the frame (bm masks them out of every use
   // of col as a column set), so a saved frame is exactly {ld, rd, col, avail}
-  uint32_t ld = 0, rd = 0, col = 0, avail = 0, bm = 0, sp = 0;
+  uint32_t ld = 0, rd = 0, col = 0, avail = 0, bm = 0;
+  uint32_t sp = 0;      // shared address of the next free frame of this lane's stack
+  uint32_t sbase = 0;   // shared address of its first frame: the stack is empty when sp == sbase
   typename std::conditional<BIG, unsigned long long, uint32_t>::type cnt = 0;
 
-  // sp is the byte offset of the next free frame in this lane's interleaved stack
   template <int BLOCK>
-  __device__ __forceinline__ void step(unsigned char* stk, const typename WordT<WIDE>::type* sch) {
-    if (avail == 0 && sp != 0) {
-      sp -= BLOCK * (uint32_t)sizeof(uint4);
-      const uint4 f = *reinterpret_cast<const uint4*>(stk + sp);
-      ld = f.x; rd = f.y; col = f.z; avail = f.w;
-    }
+  __device__ __forceinline__ void step(uint32_t sch) {
+    using W = typename WordT<WIDE>::type;
+    constexpr uint32_t F = BLOCK * (uint32_t)sizeof(uint4);
+    const uint32_t pop = (avail == 0u && sp != sbase) ? 1u : 0u;
+    sp -= pop ? F : 0u;
+    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %4, 0;\n\t@p ld.shared.v4.u32 {%0, %1, %2, %3}, [%5];\n\t}"
+                 : "+r"(ld), "+r"(rd), "+r"(col), "+r"(avail) : "r"(pop), "r"(sp));
     const uint32_t d = col >> 27;
     const bool act = avail != 0;
     const uint32_t bit = avail & (0u - avail);
     avail -= bit;
-    const Dec o = decode(sch[d * BLOCK]);
+    const Dec o = decode(lds_word(sch + d * (BLOCK * (uint32_t)sizeof(W)), W{}));
     const uint32_t nld = ((ld + bit) << o.s) | o.la;
     const uint32_t nrd = ((rd + bit) >> o.s) | o.ra;
     const uint32_t ncol = col + bit;
@@ -310,10 +326,10 @@ struct Lane {
     if constexpr (WIDE) hit = hit || (act && o.term && o.tall);
     cnt += hit ? 1u : 0u;
     const bool desc = live && !o.term && !(o.fc && ahead == 0u);
-    if (desc && avail != 0u) {
-      *reinterpret_cast<uint4*>(stk + sp) = make_uint4(ld, rd, col, avail);
-      sp += BLOCK * (uint32_t)sizeof(uint4);
-    }
+    const uint32_t push = (desc && avail != 0u) ? 1u : 0u;
+    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %0, 0;\n\t@p st.shared.v4.u32 [%1], {%2, %3, %4, %5};\n\t}"
+                 :: "r"(push), "r"(sp), "r"(ld), "r"(rd), "r"(col), "r"(avail) : "memory");
+    sp += push ? F : 0u;
     if (desc) { ld = nld; rd = nrd; col = ncol + (1u << 27); avail = nf; }
   }
 };
@@ -327,15 +343,16 @@ __global__ void __launch_bounds__(BLOCK) dfs_kernel(const DfsArgs a) {
   const unsigned lane = threadIdx.x & 31u;
   const unsigned lt_mask = (1u << lane) - 1u;
   const W* __restrict__ gsched = reinterpret_cast<const W*>(a.sched);
-  unsigned char* stkb = reinterpret_cast<unsigned char*>(stk);   // this lane's stack, byte-addressed
   Lane<WIDE, BIG> L;
+  L.sbase = L.sp = (uint32_t)__cvta_generic_to_shared(stk);
+  const uint32_t sch_sh = (uint32_t)__cvta_generic_to_shared(sch);
   uint32_t wexp = 0, job = a.job_base, task = 0;
   bool have = false, exhausted = false;
   unsigned long long acc = 0;
   uint32_t acc_job = a.job_base;
 
   for (;;) {
-    const bool idle = (L.avail | L.sp) == 0u;
+    const bool idle = (L.avail | (L.sp - L.sbase)) == 0u;
     if (__ballot_sync(FULL, idle)) {          // some lane finished: flush, refill, maybe exit
       if (idle && have) {
         const unsigned long long v = (unsigned long long)L.cnt << wexp;
@@ -369,7 +386,7 @@ __global__ void __launch_bounds__(BLOCK) dfs_kernel(const DfsArgs a) {
             wexp = info_wexp(in.x);
             job = in.y;
             L.bm = (1u << info_N(in.x)) - 1u;
-            L.sp = 0;
+            L.sp = L.sbase;
             if (T == INFO_NO_DFS || info_status(in.x) != TS_OK || T < d0) {
               L.avail = 0;
             } else if ((int)(T - d0) > a.maxt) {    // frames at depths 0..T'-1, words 0..T'
@@ -385,10 +402,11 @@ __global__ void __launch_bounds__(BLOCK) dfs_kernel(const DfsArgs a) {
           }
         }
       }
-      if (__all_sync(FULL, exhausted && (L.avail | L.sp) == 0u)) break;
+      if (__all_sync(FULL, exhausted && (L.avail | (L.sp - L.sbase)) == 0u)) break;
+      asm volatile("" ::: "memory");   // refill stores to the schedule before the steps' loads
     }
 #pragma unroll kStepUnroll
-    for (int s = 0; s < kStepsPerCheck; ++s) L.template step<BLOCK>(stkb, sch);
+    for (int s = 0; s < kStepsPerCheck; ++s) L.template step<BLOCK>(sch_sh);
   }
 
   const uint32_t j0 = __shfl_sync(FULL, acc_job, 0);

@@ -51,7 +51,7 @@ class _InFlight:
 
 
 # GPU milliseconds of a whole-board count on GB300 (measured with bench-style timing).
-_COUNT_MS = {16: 1.4, 17: 5.4, 18: 26.0, 19: 143.0, 20: 1190.0, 21: 9500.0}
+_COUNT_MS = {16: 0.9, 17: 3.0, 18: 16.0, 19: 108.0, 20: 860.0, 21: 7300.0}
 
 
 def estimate_ms(job) -> float:
