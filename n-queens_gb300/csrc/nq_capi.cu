@@ -606,23 +606,30 @@ int nq_batch_create(nq_handle* h, const nq_job* jobs, int njobs, nq_batch** out)
   std::vector<nq_record> recs;
   std::vector<HostTask> htasks;
   std::vector<int64_t> job_host_begin(njobs, -1), job_host_end(njobs, -1);
+  // The generator is deterministic in (N, preset): jobs that repeat a pair reuse
+  // its records (each job still gets its own task segment and job id).
+  struct Gen { std::vector<GenRecord> v; int smin; };
+  std::map<std::pair<int, int>, Gen> generated;
   int maxt = 1;
   for (int j = 0; j < njobs; j++) {
     const nq_job& J = jobs[j];
     if (J.N < 1 || J.N > kMaxN || J.k < 0 || J.k > 8) { nq_batch_destroy(b); return h->fail(NQ_EINVAL, "batch job %d: bad N or k", j); }
     if (J.kind == NQ_JOB_COUNT && J.N >= 6) {
       const int p = J.preset > 0 ? J.preset : preset_for(J.N);
-      std::vector<GenRecord> v;
-      const int s = gen_constellations(J.N, p, v, 0);
-      if (s != 0) { nq_batch_destroy(b); return h->fail(s == -2 ? NQ_EPRESET : NQ_EINVAL, "batch job %d: generator failed", j); }
-      Seg sg{j, J.N, (int64_t)recs.size(), (int64_t)v.size()};
-      int smin = 64;
-      for (auto& g : v) {
-        recs.push_back(nq_record{(uint32_t)g.ld, (uint32_t)g.rd, (uint32_t)g.col, g.startijkl});
-        smin = std::min<int>(smin, (int)(g.startijkl >> 20));
+      auto it = generated.find({J.N, p});
+      if (it == generated.end()) {
+        Gen g;
+        const int s = gen_constellations(J.N, p, g.v, 0);
+        if (s != 0) { nq_batch_destroy(b); return h->fail(s == -2 ? NQ_EPRESET : NQ_EINVAL, "batch job %d: generator failed", j); }
+        g.smin = 64;
+        for (auto& r : g.v) g.smin = std::min<int>(g.smin, (int)(r.startijkl >> 20));
+        it = generated.emplace(std::make_pair(J.N, p), std::move(g)).first;
       }
+      const std::vector<GenRecord>& v = it->second.v;
+      Seg sg{j, J.N, (int64_t)recs.size(), (int64_t)v.size()};
+      for (auto& g : v) recs.push_back(nq_record{(uint32_t)g.ld, (uint32_t)g.rd, (uint32_t)g.col, g.startijkl});
       segs.push_back(sg);
-      b->job_maxt[j] = maxt_for(J.N, smin);
+      b->job_maxt[j] = maxt_for(J.N, it->second.smin);
       maxt = std::max(maxt, b->job_maxt[j]);
     } else if (J.kind == NQ_JOB_COUNT || J.kind == NQ_JOB_COMPLETION) {
       int rows[8], cols[8];

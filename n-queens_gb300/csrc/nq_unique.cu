@@ -31,6 +31,7 @@ namespace {
 
 constexpr unsigned FULLM = 0xFFFFFFFFu;
 constexpr int kBoardWords = 8;   // rows of the board prefix carried by a task
+constexpr int kUniqueSteps = 16;   // steps per lane between checks for finished lanes
 
 // One start configuration (symmetry part and its bounds).
 struct UConf {
@@ -144,31 +145,36 @@ __global__ void __launch_bounds__(BLOCK) unique_kernel(const UArgs a) {
       }
       if (__all_sync(FULLM, exhausted && (avail | sp) == 0u)) break;
     }
-    if (avail == 0u && sp != 0u) {
-      --sp;
-      const uint4 f = stk[sp * BLOCK];
-      left = f.x; down = f.y; right = f.z; avail = f.w & 0x07FFFFFFu; row = f.w >> 27;
-    }
-    if (avail != 0u) {
-      const uint32_t bit = avail & (0u - avail);
-      avail -= bit;
-      brd[row * BLOCK] = bit;
-      const uint32_t nl = (left | bit) << 1, nd = down | bit, nr = (right | bit) >> 1;
-      const uint32_t nrow = row + 1;
-      uint32_t nb = mask & ~(nl | nd | nr);
-      if (nrow == (uint32_t)N - 1u) {                   // last row: a solution or none
-        if (cf.part == 1) {
-          if (nb) c8++;
-        } else if (nb && (nb & cf.lastmask) == 0u) {
-          brd[nrow * BLOCK] = nb;
-          const uint32_t k = classify([&](int r) { return brd[r * BLOCK]; }, N, cf);
-          c2 += (k == 2); c4 += (k == 4); c8 += (k == 8);
-        }
-      } else {
-        nb = row_filter(nb, nrow, nd, cf);
-        if (nb) {
-          if (avail) { stk[sp * BLOCK] = make_uint4(left, down, right, avail | (row << 27)); ++sp; }
-          left = nl; down = nd; right = nr; avail = nb; row = nrow;
+    // kUniqueSteps steps between two checks for finished lanes (two ballots each); not
+    // unrolled: the leaf classification makes the step long
+#pragma unroll 1
+    for (int s = 0; s < kUniqueSteps; ++s) {
+      if (avail == 0u && sp != 0u) {
+        --sp;
+        const uint4 f = stk[sp * BLOCK];
+        left = f.x; down = f.y; right = f.z; avail = f.w & 0x07FFFFFFu; row = f.w >> 27;
+      }
+      if (avail != 0u) {
+        const uint32_t bit = avail & (0u - avail);
+        avail -= bit;
+        brd[row * BLOCK] = bit;
+        const uint32_t nl = (left | bit) << 1, nd = down | bit, nr = (right | bit) >> 1;
+        const uint32_t nrow = row + 1;
+        uint32_t nb = mask & ~(nl | nd | nr);
+        if (nrow == (uint32_t)N - 1u) {                   // last row: a solution or none
+          if (cf.part == 1) {
+            if (nb) c8++;
+          } else if (nb && (nb & cf.lastmask) == 0u) {
+            brd[nrow * BLOCK] = nb;
+            const uint32_t k = classify([&](int r) { return brd[r * BLOCK]; }, N, cf);
+            c2 += (k == 2); c4 += (k == 4); c8 += (k == 8);
+          }
+        } else {
+          nb = row_filter(nb, nrow, nd, cf);
+          if (nb) {
+            if (avail) { stk[sp * BLOCK] = make_uint4(left, down, right, avail | (row << 27)); ++sp; }
+            left = nl; down = nd; right = nr; avail = nb; row = nrow;
+          }
         }
       }
     }

@@ -164,6 +164,46 @@ def test_schedule_replay_matches_oracle(nq, oracle_mod, N, preset):
         assert nd <= int(nodes[i])   # pruning may only remove work
 
 
+@pytest.mark.parametrize("N", [10, 12, 13])
+def test_lookahead_on_every_sound_word(nq, oracle_mod, N):
+    """The schedule builder sets the look-ahead flag on every word whose child step is one row and not a
+    tall terminal (the rule that makes the prune count-preserving), and the replay with those flags still
+    gives the oracle's per-record counts with fewer or equal nodes."""
+    o = oracle_mod.gen_constellations(N, 5)
+    sol, nodes = oracle_mod.exec_solutions(N, o, threads=1, want_nodes=True)
+    rec = np.zeros(len(o), nq.RECORD_DTYPE)
+    rec["ld"] = o.ld & M32; rec["rd"] = o.rd & M32; rec["col"] = o.col & M32; rec["startijkl"] = o.startijkl
+    flagged = fewer = 0
+    for i in range(len(o)):
+        root, info, words = schedule_of(rec[i], N)
+        T = info & 31
+        if T == 31:
+            continue
+        for d in range(T):
+            child = words[d + 1]
+            if (child >> 29) == 1 and not (child & (1 << 28)):
+                assert words[d] & (1 << 25), (i, d, hex(words[d]), hex(child))
+                flagged += 1
+        got, nd = replay(root, info, words, wide=False)
+        assert got == int(sol[i])
+        fewer += nd < int(nodes[i])
+    assert flagged > 0 and fewer > 0
+
+
+def test_completion_lookahead_flags(nq):
+    """Completion schedules: look-ahead on every word whose child is a one-row, non-tall step; never on the
+    parent of the tall last row."""
+    for queens in ([(0, 1)], [(2, 5), (7, 3)], [(5, 0)]):
+        for root, info, w in completion_tasks(12, queens):
+            T = info & 31
+            if T == 31:
+                continue
+            for d in range(T):
+                x1 = w[d + 1][0]
+                sound = ((x1 >> 24) & 7) == 1 and not (x1 & (1 << 30))
+                assert bool(w[d][0] & (1 << 27)) == sound, (queens, d)
+
+
 def completion_tasks(N, queens, min_tasks=64):
     from nqueens import _lib
     k = len(queens)
