@@ -172,8 +172,9 @@ namespace {
 
 
 // records (device) -> counts on st; totals land in ctrl[0].  Launches
-// prepare, then (when splitting) the split count pass, one 8-byte read-back
-// to size the subtask queue, the split write pass, and the DFS.
+// prepare, then (when splitting) the split count pass, one read-back of the
+// control block (subtask count and deepest schedule), the split write pass,
+// and the DFS with a stack sized to the deepest subtask.
 int run_records(nq_handle* h, int N, const uint4* d_rec, int64_t m, int start_min, unsigned long long* d_per_task,
                 cudaStream_t st) {
   const int maxt = maxt_for(N, start_min);
@@ -191,8 +192,9 @@ int run_records(nq_handle* h, int N, const uint4* d_rec, int64_t m, int start_mi
   unsigned int* cursor = (unsigned int*)(c + 8);
   unsigned int* err = (unsigned int*)(c + 12);
   unsigned long long* sctr = (unsigned long long*)(c + 16);   // split: [0] subtasks, [1] allocation cursor
+  unsigned int* tmax = (unsigned int*)(c + 32);                // deepest schedule of the launch
   NQ_CUDA(h, cudaEventRecord(h->ev[0], st));
-  NQ_CUDA(h, launch_prepare(N, m, d_rec, ta, 0, 0, err, st));
+  NQ_CUDA(h, launch_prepare(N, m, d_rec, ta, 0, 0, err, st, tmax));
   const int D = h->split >= 0 ? h->split : choose_split(m, h->sms);
   DfsLaunch L;
   L.tasks = ta; L.m = m; L.order = nullptr; L.cursor = cursor; L.job_totals = totals;
@@ -200,9 +202,16 @@ int run_records(nq_handle* h, int N, const uint4* d_rec, int64_t m, int start_mi
   if (D > 0) {
     NQ_CUDA(h, h->nsub.ensure((size_t)m * sizeof(uint32_t)));
     NQ_CUDA(h, launch_split(0, D, 0, m, ta, (uint32_t*)h->nsub.p, nullptr, nullptr, sctr, nullptr, totals, 0, st));
-    if (int s = h->ensure_pinned(Ctrl::bytes(1) + 16)) return s;
-    NQ_CUDA(h, cudaMemcpyAsync(h->h_ctrl, c, Ctrl::bytes(1) + 16, cudaMemcpyDeviceToHost, st));
-    NQ_CUDA(h, cudaStreamSynchronize(st));
+  }
+  // One read-back: the split size and the deepest schedule T.  Subtasks start
+  // at depth D with an empty stack, so the DFS needs T - D frames and T - D + 1
+  // schedule words per lane; the kernel still rejects any task deeper than that.
+  if (int s = h->ensure_pinned(Ctrl::bytes(1) + 16)) return s;
+  NQ_CUDA(h, cudaMemcpyAsync(h->h_ctrl, c, Ctrl::bytes(1) + 16, cudaMemcpyDeviceToHost, st));
+  NQ_CUDA(h, cudaStreamSynchronize(st));
+  const int t_deep = (int)(uint32_t)h->h_ctrl[4];
+  L.maxt = std::max(1, std::min(maxt, t_deep - D));
+  if (D > 0) {
     const int64_t ns = (int64_t)h->h_ctrl[2];
     if (ns > (int64_t)0xFFFFFFFF) return h->fail(NQ_ENOMEM, "split: %lld subtasks", (long long)ns);
     NQ_CUDA(h, h->sroot.ensure((size_t)std::max<int64_t>(ns, 1) * sizeof(uint4)));
@@ -680,12 +689,20 @@ int nq_batch_create(nq_handle* h, const nq_job* jobs, int njobs, nq_batch** out)
   unsigned int* derr = (unsigned int*)(c + (size_t)njobs * 8 + 4);
   cudaStream_t st = b->stream;
   int status = NQ_OK;
+  DevBuf jt;                                   // deepest schedule per job (constellation jobs)
+  jt.ordered = st;
+  std::vector<uint32_t> job_deep(njobs, 0);
   do {
     if ((e = cudaMemsetAsync(c, 0, cb, st)) != cudaSuccess) break;
+    if ((e = jt.ensure((size_t)njobs * sizeof(uint32_t))) != cudaSuccess) break;
+    if ((e = cudaMemsetAsync(jt.p, 0, (size_t)njobs * sizeof(uint32_t), st)) != cudaSuccess) break;
     if (m_rec && (e = cudaMemcpyAsync(b->rec.p, recs.data(), (size_t)m_rec * sizeof(nq_record), cudaMemcpyHostToDevice, st)) != cudaSuccess) break;
     for (auto& sg : segs)
-      if ((e = launch_prepare(sg.N, sg.m, (const uint4*)b->rec.p + sg.rec_off, ta, sg.rec_off, (uint32_t)sg.job, derr, st)) != cudaSuccess) break;
+      if ((e = launch_prepare(sg.N, sg.m, (const uint4*)b->rec.p + sg.rec_off, ta, sg.rec_off, (uint32_t)sg.job, derr, st,
+                              (unsigned int*)jt.p + sg.job)) != cudaSuccess) break;
     if (e != cudaSuccess) break;
+    if ((e = cudaMemcpyAsync(job_deep.data(), jt.p, (size_t)njobs * sizeof(uint32_t), cudaMemcpyDeviceToHost, st)) !=
+        cudaSuccess) break;
     if (m_host) {
       std::vector<uint4> hr(m_host);
       std::vector<uint2> hi(m_host);
@@ -729,6 +746,14 @@ int nq_batch_create(nq_handle* h, const nq_job* jobs, int njobs, nq_batch** out)
     int64_t total_sub = 0;
     for (int j = 0; j < njobs; j++) { b->sub_off[j] = total_sub; b->sub_m[j] = (int64_t)cnts[2 * j]; total_sub += b->sub_m[j]; }
     b->ms = total_sub;
+    // Stacks sized to the deepest subtask: a job's subtasks start at depth
+    // job_split[j], so they need (deepest T) - job_split[j] frames.
+    b->maxt = 1;
+    for (int j = 0; j < njobs; j++) {
+      const int deep = (job_host_begin[j] >= 0) ? b->job_maxt[j] : (int)job_deep[j];
+      b->job_maxt[j] = std::max(1, std::min(b->job_maxt[j], deep - b->job_split[j]));
+      b->maxt = std::max(b->maxt, b->job_maxt[j]);
+    }
     if ((e = b->sroot.ensure((size_t)std::max<int64_t>(total_sub, 1) * sizeof(uint4))) != cudaSuccess ||
         (e = b->sinfo.ensure((size_t)std::max<int64_t>(total_sub, 1) * sizeof(uint2))) != cudaSuccess) { sctr.release(); break; }
     // settled counts of small tasks land in the control block's totals (zeroed above)
@@ -743,6 +768,7 @@ int nq_batch_create(nq_handle* h, const nq_job* jobs, int njobs, nq_batch** out)
     b->device_bytes = (int64_t)(b->root.cap + b->info.cap + b->sched.cap + b->rec.cap + b->ctrl.cap + b->nsub.cap +
                                 b->sroot.cap + b->sinfo.cap);
   } while (0);
+  jt.release();
   if (e != cudaSuccess) status = h->cuda_fail(e, "batch build");
   if (status != NQ_OK) { nq_batch_destroy(b); return status; }
   *out = b;

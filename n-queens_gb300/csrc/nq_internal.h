@@ -43,8 +43,9 @@ struct DfsLaunch {
 // Prepare: records {ld, rd, col, startijkl} (the reference's 16-byte task
 // record) -> task arrays.  job/offset place the tasks of one job inside a
 // larger queue.
+// tmax (optional): atomicMax of the schedule depth T over the launch's tasks.
 cudaError_t launch_prepare(int N, int64_t m, const uint4* records, const TaskArrays& out, int64_t offset,
-                           uint32_t job, unsigned int* err, cudaStream_t st);
+                           uint32_t job, unsigned int* err, cudaStream_t st, unsigned int* tmax = nullptr);
 
 cudaError_t launch_dfs(const DfsLaunch& L, cudaStream_t st);
 

@@ -48,12 +48,9 @@ template <> struct WordT<true> { using type = uint2; };
 // prepare
 // ---------------------------------------------------------------------------
 template <bool WIDE>
-__global__ void __launch_bounds__(256) prepare_kernel(int N, int64_t m, const uint4* __restrict__ rec,
-                                                      uint4* __restrict__ root, uint2* __restrict__ info,
-                                                      typename WordT<WIDE>::type* __restrict__ sched, int sw,
-                                                      int64_t offset, uint32_t job, unsigned int* err) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= m) return;
+__device__ __forceinline__ int prepare_one(int N, const uint4* __restrict__ rec, uint4* __restrict__ root,
+                                           uint2* __restrict__ info, typename WordT<WIDE>::type* __restrict__ sched,
+                                           int sw, int64_t offset, uint32_t job, unsigned int* err, int64_t i) {
   const uint4 r = rec[i];
   const int64_t t = offset + i;
   uint32_t status = TS_OK;
@@ -89,18 +86,35 @@ __global__ void __launch_bounds__(256) prepare_kernel(int N, int64_t m, const ui
       else s[d] = pack_compact(ops[d]);
     }
   }
+  return T;
 }
 
+template <bool WIDE>
+__global__ void __launch_bounds__(256) prepare_kernel(int N, int64_t m, const uint4* __restrict__ rec,
+                                                      uint4* __restrict__ root, uint2* __restrict__ info,
+                                                      typename WordT<WIDE>::type* __restrict__ sched, int sw,
+                                                      int64_t offset, uint32_t job, unsigned int* err,
+                                                      unsigned int* tmax) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int T = (i < m) ? prepare_one<WIDE>(N, rec, root, info, sched, sw, offset, job, err, i) : -1;
+  if (tmax) {                         // deepest schedule of the launch, for sizing the DFS stack
+    const unsigned v = __reduce_max_sync(FULL, (unsigned)(T < 0 ? 0 : T));
+    if ((threadIdx.x & 31u) == 0 && v) atomicMax(tmax, v);
+  }
+}
+
+
 cudaError_t launch_prepare(int N, int64_t m, const uint4* records, const TaskArrays& out, int64_t offset,
-                           uint32_t job, unsigned int* err, cudaStream_t st) {
+                           uint32_t job, unsigned int* err, cudaStream_t st, unsigned int* tmax) {
   if (m <= 0) return cudaSuccess;
   const int B = 256;
   const unsigned G = (unsigned)((m + B - 1) / B);
   if (out.wide)
-    prepare_kernel<true><<<G, B, 0, st>>>(N, m, records, out.root, out.info, (uint2*)out.sched, out.sw, offset, job, err);
+    prepare_kernel<true><<<G, B, 0, st>>>(N, m, records, out.root, out.info, (uint2*)out.sched, out.sw, offset, job, err,
+                                          tmax);
   else
     prepare_kernel<false><<<G, B, 0, st>>>(N, m, records, out.root, out.info, (uint32_t*)out.sched, out.sw, offset, job,
-                                           err);
+                                           err, tmax);
   return cudaGetLastError();
 }
 
