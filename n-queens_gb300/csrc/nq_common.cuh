@@ -47,7 +47,7 @@ constexpr uint32_t C_FC = 1u << 25;
 constexpr uint32_t C_TERM = 1u << 26;
 constexpr uint32_t C_B14 = 1u << 27;
 constexpr uint32_t C_TALL = 1u << 28;
-constexpr int C_SSHIFT = 29;
+constexpr int C_SSHIFT = 29;   // s in 1..3: walk_schedule steps 1, 2 or 3 rows (the DFS forms 1 << s as s*s - s + 2)
 // wide word fields (x)
 constexpr uint32_t W_LA = 0x00FFFFFFu;
 constexpr int W_SSHIFT = 24;
@@ -272,7 +272,5 @@ NQ_HD uint32_t pack_wide_x(const Op& o) {
   return (o.la & W_LA) | (o.s << W_SSHIFT) | (o.fc ? W_FC : 0u) | (o.term ? W_TERM : 0u) | (o.b14 ? W_B14 : 0u) |
          (o.tall ? W_TALL : 0u);
 }
-// The compact word can hold the op only if LA fits bits 0-1 and RA bits 2-24.
-NQ_HD bool fits_compact(const Op& o) { return (o.la & ~C_LA) == 0 && (o.ra & ~C_RA) == 0 && o.s <= 7; }
 
 }  // namespace nq

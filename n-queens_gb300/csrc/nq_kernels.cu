@@ -129,6 +129,13 @@ __device__ __forceinline__ Dec decode(uint2 w) {
   return Dec{(w.x >> W_SSHIFT) & 7u, w.x & W_LA, w.y, w.x & W_FC, w.x & W_TERM, w.x & W_B14, w.x & W_TALL};
 }
 
+// The same decode with the shift field taken by a multiply-high, which issues
+// on the FMA pipe instead of the integer ALU pipe (the DFS step's binding pipe).
+__device__ __forceinline__ Dec decode_fma(uint32_t w) {
+  return Dec{__umulhi(w, 1u << (32 - C_SSHIFT)), w & C_LA, w & C_RA, w & C_FC, w & C_TERM, w & C_B14, w & C_TALL};
+}
+__device__ __forceinline__ Dec decode_fma(uint2 w) { return decode(w); }
+
 // ---------------------------------------------------------------------------
 // split: expand every task to depth D (1..3) so the DFS queue holds many
 // small subtasks instead of few large ones (the reference's measured
@@ -322,17 +329,21 @@ struct Lane {
     sp -= pop ? F : 0u;
     asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %4, 0;\n\t@p ld.shared.v4.u32 {%0, %1, %2, %3}, [%5];\n\t}"
                  : "+r"(ld), "+r"(rd), "+r"(col), "+r"(avail) : "r"(pop), "r"(sp));
-    const uint32_t d = col >> 27;
+    const uint32_t d = __umulhi(col, 32u);          // col >> 27, on the FMA pipe
     const bool act = avail != 0;
     const uint32_t bit = avail & (0u - avail);
     avail -= bit;
-    const Dec o = decode(lds_word(sch + d * (BLOCK * (uint32_t)sizeof(W)), W{}));
-    const uint32_t nld = ((ld + bit) << o.s) | o.la;
+    const W w = lds_word(sch + d * (BLOCK * (uint32_t)sizeof(W)), W{});
+    const Dec o = decode_fma(w);
+    uint32_t nld;
+    if constexpr (WIDE) nld = ((ld + bit) << o.s) | o.la;
+    else nld = (ld + bit) * (o.s * (o.s - 1u) + 2u) + o.la;   // (x << s) | la: s*s - s + 2 = 1 << s for the
+                                                               // compact word's s in 1..3, la lies below bit s
     const uint32_t nrd = ((rd + bit) >> o.s) | o.ra;
     const uint32_t ncol = col + bit;
     const uint32_t free_cols = bm & ~ncol;
     const uint32_t nf = free_cols & ~(nld | nrd);
-    const uint32_t ahead = free_cols & ~((nld + nld) | (nrd >> 1));
+    const uint32_t ahead = free_cols & ~((nld + nld) | __umulhi(nrd, 0x80000000u));   // nrd >> 1
     // terminal depth: count the child (the SQd2B rule is LA bit 0 of the word);
     // otherwise descend unless the child row or, with look-ahead, the row after is full
     const bool live = act && nf != 0u;

@@ -204,6 +204,26 @@ def test_completion_lookahead_flags(nq):
                 assert bool(w[d][0] & (1 << 27)) == sound, (queens, d)
 
 
+@pytest.mark.parametrize("N,preset", [(n, p) for n in (8, 11, 14) for p in (4, 5, 6, 7)])
+def test_compact_words_step_one_to_three_rows(nq, oracle_mod, N, preset):
+    """Compact schedule words step 1, 2 or 3 rows and keep la below bit s: the DFS kernel forms 1 << s as
+    s*s - s + 2 and adds la instead of or-ing it, both exact only under these bounds."""
+    try:
+        o = oracle_mod.gen_constellations(N, preset)
+    except ValueError:
+        pytest.skip("the reference raises for this preset (negative shift)")
+    rec = np.zeros(len(o), nq.RECORD_DTYPE)
+    rec["ld"] = o.ld & M32; rec["rd"] = o.rd & M32; rec["col"] = o.col & M32; rec["startijkl"] = o.startijkl
+    seen = set()
+    for i in range(len(o)):
+        _, info, words = schedule_of(rec[i], N)
+        for w in words:
+            s = w >> 29
+            assert 1 <= s <= 3 and (w & 3) < (1 << s), (i, hex(w))
+            seen.add(s)
+    assert not seen or 1 in seen
+
+
 def completion_tasks(N, queens, min_tasks=64):
     from nqueens import _lib
     k = len(queens)
