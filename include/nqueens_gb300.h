@@ -170,6 +170,10 @@ int nq_batch_set_grid(nq_batch *b, int grid);
 /* Resident DFS blocks on the whole GPU for the handle's block size and a stack
  * of maxt frames (wide: batch schedule words). */
 int nq_resident_blocks(nq_handle *h, int wide, int maxt, int *blocks);
+/* Resident DFS blocks on the whole GPU for this batch's own launch (its block
+ * size, schedule word and stack depth): the unit nq_batch_set_grid shares out.
+ * No counterpart in the reference (it runs one N per process). */
+int nq_batch_resident_blocks(const nq_batch *b, int *blocks);
 int64_t nq_batch_device_bytes(const nq_batch *b);
 /* All jobs in one persistent launch (use_graph: replay a captured CUDA graph). */
 int nq_batch_run(nq_batch *b, int use_graph, uint64_t *totals);

@@ -78,15 +78,18 @@ const char* derr_text(uint32_t e) {
 
 // Expand tasks until the queue holds at least 13 items per resident DFS lane
 // (the DFS kernel keeps about 768 lanes per SM), at most 3 levels.  Each level
-// multiplies the queue by about 7 (measured: 6.2x at N=16 to 8x at N=20);
-// this rule picks the depth the autotuner found fastest on GB300 for N=16..20
-// (2, 2, 1, 1, 1).
+// multiplies the queue by about 7 (measured: 6.2x at N=16 to 8x at N=20).
+// Task lists of a million or more are split at least once: their largest
+// tasks set the tail (GB300, N=21: D=0 7466 ms, D=1 6983 ms, D=2 6914 ms).
+// This rule picks the depth the autotuner found fastest on GB300 for
+// N=16..21 (2, 2, 1, 1, 1-2, 1-2).
 int choose_split(int64_t m, int sms) {
   const double target = 13.0 * 768.0 * (double)sms;
   int D = 0;
   double est = (double)m;
   while (D < 3 && est < target) { est *= 7.0; D++; }
-  return D;
+  // ~7 subtasks per task must stay within the u32 subtask queue
+  return (D == 0 && m >= 1000000 && m <= 400000000) ? 1 : D;
 }
 
 int maxt_for(int N, int start_min) {
@@ -786,6 +789,12 @@ int nq_batch_set_grid(nq_batch* b, int grid) {
 int nq_resident_blocks(nq_handle* h, int wide, int maxt, int* blocks) {
   if (!h || !blocks || maxt < 1 || maxt >= kMaxDepth) return NQ_EINVAL;
   *blocks = h->sms * std::max(1, dfs_blocks_per_sm(wide != 0, h->block, maxt));
+  return NQ_OK;
+}
+
+int nq_batch_resident_blocks(const nq_batch* b, int* blocks) {
+  if (!b || !blocks) return NQ_EINVAL;
+  *blocks = b->h->sms * std::max(1, dfs_blocks_per_sm(b->wide, b->block, b->maxt));
   return NQ_OK;
 }
 

@@ -167,6 +167,12 @@ class Batch:
     def device_bytes(self) -> int:
         return int(lib().nq_batch_device_bytes(self._b))
 
+    def resident_blocks(self) -> int:
+        """DFS blocks resident on the whole GPU for this batch's launch (what set_grid shares out)."""
+        v = ctypes.c_int()
+        _check(lib().nq_batch_resident_blocks(self._b, ctypes.byref(v)), self.engine._h, "batch resident_blocks")
+        return v.value
+
     def set_grid(self, grid: int) -> None:
         """Blocks of this batch's persistent launch (0: every resident block of the GPU)."""
         _check(lib().nq_batch_set_grid(self._b, int(grid)), self.engine._h, "batch set_grid")

@@ -39,6 +39,9 @@ class _Request:
     job: object
     future: Future
     t_arrival: float
+    seq: int = 0
+    t_admit: float = 0.0    # taken off the queue into a batch
+    t_built: float = 0.0    # its batch built and launched
     t_done: float = 0.0
 
 
@@ -81,6 +84,8 @@ def _bytes_estimate(job) -> int:
 class ServerStats:
     completed: int
     latencies_s: List[float] = field(default_factory=list)
+    latencies_by_request: List[float] = field(default_factory=list)   # in submission order
+    phases_by_request: List[tuple] = field(default_factory=list)      # (queued, build, run) seconds
     makespan_s: float = 0.0
     batches: int = 0
     max_inflight_seen: int = 0
@@ -98,14 +103,15 @@ class Server:
 
     def __init__(self, device: int = 0, budget_bytes: int = 16 << 30, max_inflight: int = 3,
                  max_batch_jobs: int = 64, use_graph: bool = False, engine: Optional[Engine] = None,
-                 poll_us: int = 200, share_gpu: bool = True, large_ms: float = 10.0, large_share: float = 0.875):
+                 poll_us: int = 200, share_gpu: bool = True, large_ms: float = 50.0, large_share: float = 0.875):
         self.engine = engine or Engine(device)
         # Lanes: requests estimated above large_ms run one per batch on large_share of the
         # resident blocks; the rest are batched on the remaining share (share_gpu), so a
-        # small request admitted while a large one runs starts at once beside it.
-        full = self.engine.resident_blocks()
-        self._grid_large = max(1, int(full * large_share)) if share_gpu else 0
-        self._grid_small = max(1, full - self._grid_large) if share_gpu else 0
+        # small request admitted while a large one runs starts at once beside it.  Shares
+        # are taken of each batch's own resident capacity (its stack depth sets how many
+        # blocks fit on an SM).
+        self.share_gpu = bool(share_gpu)
+        self.large_share = float(large_share)
         self.large_ms = float(large_ms)
         self.budget = int(budget_bytes)
         self.max_inflight = int(max_inflight)
@@ -116,6 +122,7 @@ class Server:
         self._pending_large: Deque[_Request] = collections.deque()  # large requests
         self._inflight: List[_InFlight] = []
         self._building = 0
+        self._seq = 0
         self._admitted = 0
         self._cv = threading.Condition()
         self._stop = False
@@ -139,7 +146,8 @@ class Server:
                 raise RuntimeError("server stopped after an error") from self._error
             if self._t0 is None:
                 self._t0 = now
-            r = _Request(job, f, now)
+            r = _Request(job, f, now, self._seq)
+            self._seq += 1
             (self._pending_large if estimate_ms(job) > self.large_ms else self._pending).append(r)
             self._cv.notify()
         return f
@@ -159,8 +167,11 @@ class Server:
     def stats(self) -> ServerStats:
         with self._cv:
             lat = [r.t_done - r.t_arrival for r in self._done]
+            done = sorted(self._done, key=lambda r: r.seq)
+            by_req = [r.t_done - r.t_arrival for r in done]
+            phases = [(r.t_admit - r.t_arrival, r.t_built - r.t_admit, r.t_done - r.t_built) for r in done]
             span = (self._t_last - self._t0) if self._t0 is not None else 0.0
-            return ServerStats(len(self._done), lat, span, self._batches, self._max_inflight_seen)
+            return ServerStats(len(self._done), lat, by_req, phases, span, self._batches, self._max_inflight_seen)
 
     def close(self) -> None:
         with self._cv:
@@ -214,6 +225,7 @@ class Server:
                 if not take and self._inflight and self._admitted + e > self.budget:
                     return False          # wait for memory to free up
                 take.append(queue.popleft())
+                take[-1].t_admit = time.perf_counter()
                 est += e
             self._building += 1          # taken off the queue, not yet in flight
         try:
@@ -225,10 +237,13 @@ class Server:
                 self._cv.notify_all()
             return True
         nbytes = batch.device_bytes
-        grid = self._grid_large if large else self._grid_small
-        if grid:
-            batch.set_grid(grid)
+        if self.share_gpu:
+            share = self.large_share if large else 1.0 - self.large_share
+            batch.set_grid(max(1, int(round(batch.resident_blocks() * share))))
         batch.submit(self.use_graph)
+        t_built = time.perf_counter()
+        for r in take:
+            r.t_built = t_built
         with self._cv:
             self._inflight.append(_InFlight(batch, take, nbytes, large))
             self._building -= 1

@@ -16,15 +16,16 @@ def _oracle_answer(oracle_mod, job):
     return oracle_mod.completions(job.N, [r for r, _ in job.queens], [c for _, c in job.queens])
 
 
-@pytest.mark.parametrize("share_gpu,max_inflight", [(True, 3), (False, 2), (True, 1)])
-def test_server_results_exact_and_same_as_alone(oracle_mod, share_gpu, max_inflight):
+@pytest.mark.parametrize("share_gpu,max_inflight,large_ms", [(True, 3, 0.05), (False, 2, 50.0), (True, 1, 50.0)])
+def test_server_results_exact_and_same_as_alone(oracle_mod, share_gpu, max_inflight, large_ms):
     import nqueens
     from nqueens.server import Server, random_completion_queries, run_plain
     jobs = random_completion_queries(60, seed=11, N_range=(8, 13), k_range=(0, 4))
     eng = nqueens.Engine(0)
     try:
         alone = run_plain(eng, jobs)
-        with Server(engine=eng, max_inflight=max_inflight, max_batch_jobs=7, share_gpu=share_gpu) as srv:
+        with Server(engine=eng, max_inflight=max_inflight, max_batch_jobs=7, share_gpu=share_gpu,
+                    large_ms=large_ms) as srv:
             rng = np.random.default_rng(5)
             futs = []
             for j in jobs:                                  # staggered arrivals: batches overlap
@@ -63,3 +64,21 @@ def test_server_rejects_bad_request():
         f = srv.submit(nqueens.CompletionJob(8, [(0, 0), (0, 0)]))   # the same queen twice: a bad argument
         with pytest.raises(Exception):
             f.result(timeout=30)
+
+
+def test_batch_resident_blocks_and_shared_grid():
+    """A batch reports the resident capacity of its own launch (at least that of the deepest wide stack), and
+    a launch on a share of it still counts exactly."""
+    import nqueens
+    eng = nqueens.Engine(0)
+    try:
+        b = eng.batch([nqueens.CountJob(14), nqueens.CountJob(12), nqueens.CompletionJob(11, [(0, 3)])])
+        full = b.resident_blocks()
+        assert full >= eng.resident_blocks(True, 18) > 0
+        want = b.run(use_graph=False)
+        b.set_grid(max(1, full // 8))
+        assert np.array_equal(b.run(use_graph=False), want)
+        assert int(want[0]) == 365596 and int(want[1]) == 14200
+        b.close()
+    finally:
+        eng.close()
