@@ -232,8 +232,10 @@ class Engine:
         return buf.value.decode()
 
     def _apply_tuning(self, N: int) -> None:
-        if self._tuning and str(N) in self._tuning:
-            t = self._tuning[str(N)]
+        """The tuned configuration of N, or the defaults (64 threads, one wave, automatic split) for an N
+        the table does not hold, so no count inherits the previous N's settings."""
+        if self._tuning:
+            t = self._tuning.get(str(N), {"block": 64, "grid": 0, "split": -1})
             _check(lib().nq_set_config(self._h, int(t["block"]), int(t["grid"]), int(t["split"])), self._h)
 
     # -- configuration ---------------------------------------------------

@@ -67,6 +67,13 @@ def test_total_n20(eng, oracle_mod):
     assert eng.count(20).total == oracle_mod.EXPECTED_TOTAL[20] == 39029188884
 
 
+def test_total_n21_largest_configured_board(eng, oracle_mod):
+    # 2,025,282 tasks at preset 6, one split level: about 7 s on one GB300
+    r = eng.count(21)
+    assert r.total == oracle_mod.EXPECTED_TOTAL[21] == 314666222712
+    assert eng.last_run_info()[0] == 1
+
+
 def test_reference_dict_dropin(eng, oracle_mod):
     import nqueens
     _, _, cs, _ = nqueens.gen_constellations(11, set(), set(), [], 5)

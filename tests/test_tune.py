@@ -25,3 +25,18 @@ def test_autotune_small_grid_round_trip(tmp_path, oracle_mod):
             assert eng.count(N).total == oracle_mod.EXPECTED_TOTAL[N]
     finally:
         eng.close()
+
+
+def test_untuned_n_uses_defaults_not_previous_n(oracle_mod):
+    """A count of an N the tuning table does not hold runs with the default configuration, not with the
+    configuration the previous (tuned) N left behind."""
+    import nqueens
+    eng = nqueens.Engine(0)
+    try:
+        eng._tuning = {"14": {"block": 128, "grid": 0, "split": 3}}
+        assert eng.count(14).total == oracle_mod.EXPECTED_TOTAL[14]
+        assert eng.get_config() == (128, 0, 3)
+        assert eng.count(13).total == oracle_mod.EXPECTED_TOTAL[13]
+        assert eng.get_config() == (64, 0, -1)
+    finally:
+        eng.close()
