@@ -15,8 +15,9 @@
 //
 // The host expands the first rows of every (part, bound1) start into tasks;
 // the kernel is persistent, queue-fed and explicit-stack like the
-// constellation DFS (one candidate per lane per step), keeping each lane's
-// board (one bit per row) in shared memory for the leaf classification.
+// constellation DFS (one candidate per lane per step, predicated pop/push,
+// the row carried in `down`'s high bits), keeping each lane's board (one bit
+// per row) in shared memory for the leaf classification.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -109,20 +110,46 @@ struct UArgs {
   unsigned int* err;
 };
 
+// Predicated shared-memory frame load/store (32-bit shared-window addresses),
+// so the pop and the push are single predicated instructions, not branches.
+__device__ __forceinline__ void lds_frame_if(uint32_t p, uint32_t a, uint32_t& x, uint32_t& y, uint32_t& z, uint32_t& w) {
+  asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %4, 0;\n\t@q ld.shared.v4.u32 {%0, %1, %2, %3}, [%5];\n\t}"
+               : "+r"(x), "+r"(y), "+r"(z), "+r"(w) : "r"(p), "r"(a));
+}
+__device__ __forceinline__ void sts_frame_if(uint32_t p, uint32_t a, uint32_t x, uint32_t y, uint32_t z, uint32_t w) {
+  asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %0, 0;\n\t@q st.shared.v4.u32 [%1], {%2, %3, %4, %5};\n\t}"
+               :: "r"(p), "r"(a), "r"(x), "r"(y), "r"(z), "r"(w) : "memory");
+}
+__device__ __forceinline__ void sts_word_if(uint32_t p, uint32_t a, uint32_t x) {
+  asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %0, 0;\n\t@q st.shared.u32 [%1], %2;\n\t}"
+               :: "r"(p), "r"(a), "r"(x) : "memory");
+}
+
+// One lane per task, one candidate per step, all lanes on the same predicated
+// sequence: resume a saved frame, take the lowest candidate, record it in the
+// board, build the next row with the part's row rules, then count (last row)
+// or descend.  The row of a frame rides in `down` bits 27-31 (columns use bits
+// 0..N-1, N <= 27), so a saved frame is exactly {left, down, right, avail}.
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK) unique_kernel(const UArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int N = a.N;
+  constexpr uint32_t F = BLOCK * (uint32_t)sizeof(uint4);          // frame stride of one lane's stack
+  constexpr uint32_t RB = BLOCK * (uint32_t)sizeof(uint32_t);      // board row stride
   uint4* stk = reinterpret_cast<uint4*>(smem) + threadIdx.x;                            // N frames, stride BLOCK
   uint32_t* brd = reinterpret_cast<uint32_t*>(smem + (size_t)N * BLOCK * sizeof(uint4)) + threadIdx.x;  // N rows
+  const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(stk);
+  const uint32_t bbase = (uint32_t)__cvta_generic_to_shared(brd);
   const unsigned lane = threadIdx.x & 31u;
-  const uint32_t mask = (N >= 32) ? FULLM : ((1u << N) - 1u);
-  uint32_t left = 0, down = 0, right = 0, avail = 0, row = 0, sp = 0;
+  const uint32_t mask = (1u << N) - 1u;
+  const uint32_t last_row = (uint32_t)N - 1u;
+  uint32_t left = 0, down = 0, right = 0, avail = 0, sp = sbase;
   UConf cf = {0, 0, 0, 0, 0, 0, 0};
+  uint32_t lowmask = ~0u, b2 = ~0u;      // row rules of the task's part
   unsigned long long c2 = 0, c4 = 0, c8 = 0;
   bool exhausted = false;
   for (;;) {
-    const bool idle = (avail | sp) == 0u;
+    const bool idle = (avail | (sp - sbase)) == 0u;
     if (__ballot_sync(FULLM, idle)) {
       const bool want = idle && !exhausted;
       const unsigned need = __ballot_sync(FULLM, want);
@@ -136,47 +163,57 @@ __global__ void __launch_bounds__(BLOCK) unique_kernel(const UArgs a) {
           if (slot < (uint64_t)a.m) {
             const UTask t = a.tasks[slot];
             cf = a.confs[t.conf];
-            left = t.left; down = t.down; right = t.right; avail = t.avail; row = t.row; sp = 0;
+            // part 1: rows above bound1 avoid column 1; part 2: they avoid the side
+            // columns, and row bound2 is gated on the side columns used so far
+            lowmask = (cf.part == 1) ? ~2u : ~cf.sidemask;
+            b2 = (cf.part == 1) ? ~0u : cf.bound2;
+            left = t.left; down = (t.down & mask) | (t.row << 27); right = t.right; avail = t.avail; sp = sbase;
             for (uint32_t r = 0; r < t.row && r < (uint32_t)kBoardWords; r++) brd[r * BLOCK] = t.board[r];
           } else {
             exhausted = true;
           }
         }
       }
-      if (__all_sync(FULLM, exhausted && (avail | sp) == 0u)) break;
+      if (__all_sync(FULLM, exhausted && (avail | (sp - sbase)) == 0u)) break;
+      asm volatile("" ::: "memory");   // board stores of the refill before the steps' accesses
     }
-    // kUniqueSteps steps between two checks for finished lanes (two ballots each); not
-    // unrolled: the leaf classification makes the step long
+    // kUniqueSteps steps between two checks for finished lanes (two ballots each)
 #pragma unroll 1
     for (int s = 0; s < kUniqueSteps; ++s) {
-      if (avail == 0u && sp != 0u) {
-        --sp;
-        const uint4 f = stk[sp * BLOCK];
-        left = f.x; down = f.y; right = f.z; avail = f.w & 0x07FFFFFFu; row = f.w >> 27;
-      }
-      if (avail != 0u) {
-        const uint32_t bit = avail & (0u - avail);
-        avail -= bit;
-        brd[row * BLOCK] = bit;
-        const uint32_t nl = (left | bit) << 1, nd = down | bit, nr = (right | bit) >> 1;
-        const uint32_t nrow = row + 1;
-        uint32_t nb = mask & ~(nl | nd | nr);
-        if (nrow == (uint32_t)N - 1u) {                   // last row: a solution or none
-          if (cf.part == 1) {
-            if (nb) c8++;
-          } else if (nb && (nb & cf.lastmask) == 0u) {
-            brd[nrow * BLOCK] = nb;
-            const uint32_t k = classify([&](int r) { return brd[r * BLOCK]; }, N, cf);
-            c2 += (k == 2); c4 += (k == 4); c8 += (k == 8);
-          }
-        } else {
-          nb = row_filter(nb, nrow, nd, cf);
-          if (nb) {
-            if (avail) { stk[sp * BLOCK] = make_uint4(left, down, right, avail | (row << 27)); ++sp; }
-            left = nl; down = nd; right = nr; avail = nb; row = nrow;
-          }
+      const uint32_t pop = (avail == 0u && sp != sbase) ? 1u : 0u;
+      sp -= pop ? F : 0u;
+      lds_frame_if(pop, sp, left, down, right, avail);
+      const uint32_t row = __umulhi(down, 32u);                 // down >> 27
+      const bool act = avail != 0u;
+      const uint32_t bit = avail & (0u - avail);
+      avail -= bit;
+      sts_word_if(act ? 1u : 0u, bbase + row * RB, bit);        // board row `row` = the queen taken
+      const uint32_t nl = (left + bit) * 2u;
+      const uint32_t nd = down + bit;
+      const uint32_t nr = __umulhi(right + bit, 0x80000000u);   // (right | bit) >> 1
+      const uint32_t nrow = row + 1u;
+      const uint32_t nb = mask & ~(nl | nd | nr);
+      const bool last = nrow == last_row;
+      // row rules of backTrack1/backTrack2 (row_filter) as selects
+      uint32_t nbf = nb & ((nrow < cf.bound1) ? lowmask : ~0u);
+      const uint32_t ds = nd & cf.sidemask;
+      const uint32_t at_b2 = (ds == 0u) ? 0u : ((ds != cf.sidemask) ? (nbf & cf.sidemask) : nbf);
+      nbf = (nrow == b2) ? at_b2 : nbf;
+      // last row: a solution (part 1: x8) or a board to classify (part 2)
+      if (act && last && nb != 0u) {
+        if (cf.part == 1) {
+          c8++;
+        } else if ((nb & cf.lastmask) == 0u) {
+          brd[nrow * BLOCK] = nb;
+          const uint32_t k = classify([&](int r) { return brd[r * BLOCK]; }, N, cf);
+          c2 += (k == 2); c4 += (k == 4); c8 += (k == 8);
         }
       }
+      const bool desc = act && !last && nbf != 0u;
+      const uint32_t push = (desc && avail != 0u) ? 1u : 0u;
+      sts_frame_if(push, sp, left, down, right, avail);
+      sp += push ? F : 0u;
+      if (desc) { left = nl; down = nd + (1u << 27); right = nr; avail = nbf; }
     }
   }
 #pragma unroll
