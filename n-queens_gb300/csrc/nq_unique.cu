@@ -105,6 +105,7 @@ struct UArgs {
   const UConf* confs;
   int64_t m;
   int N;
+  int maxf;                     // stack frames per lane: N - 2 - (smallest task row)
   unsigned int* cursor;
   unsigned long long* counts;   // c2, c4, c8
   unsigned int* err;
@@ -136,8 +137,9 @@ __global__ void __launch_bounds__(BLOCK) unique_kernel(const UArgs a) {
   const int N = a.N;
   constexpr uint32_t F = BLOCK * (uint32_t)sizeof(uint4);          // frame stride of one lane's stack
   constexpr uint32_t RB = BLOCK * (uint32_t)sizeof(uint32_t);      // board row stride
-  uint4* stk = reinterpret_cast<uint4*>(smem) + threadIdx.x;                            // N frames, stride BLOCK
-  uint32_t* brd = reinterpret_cast<uint32_t*>(smem + (size_t)N * BLOCK * sizeof(uint4)) + threadIdx.x;  // N rows
+  // a lane pushes at most one frame per row from its task's row to N - 3
+  uint4* stk = reinterpret_cast<uint4*>(smem) + threadIdx.x;                            // maxf frames, stride BLOCK
+  uint32_t* brd = reinterpret_cast<uint32_t*>(smem + (size_t)a.maxf * BLOCK * sizeof(uint4)) + threadIdx.x;  // N rows
   const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(stk);
   const uint32_t bbase = (uint32_t)__cvta_generic_to_shared(brd);
   const unsigned lane = threadIdx.x & 31u;
@@ -315,8 +317,11 @@ extern "C" int nq_count_unique(nq_handle* h, int N, uint64_t* unique, uint64_t* 
   // 0.66 s with 32 per lane against 0.48 s, the same kernel time).
   build_unique_tasks(N, (int64_t)sms * 2048 * 2, confs, tasks);
   const int64_t m = (int64_t)tasks.size();
+  uint32_t min_row = (uint32_t)N;
+  for (const UTask& t : tasks) min_row = std::min(min_row, t.row);
+  const int maxf = std::max(1, N - 2 - (int)min_row);
   constexpr int B = 128;
-  const size_t smem = (size_t)B * N * (sizeof(uint4) + sizeof(uint32_t));
+  const size_t smem = (size_t)B * ((size_t)maxf * sizeof(uint4) + (size_t)N * sizeof(uint32_t));
   void *d_tasks = nullptr, *d_confs = nullptr, *d_ctl = nullptr;
   cudaStream_t st = nullptr;
   int status = NQ_OK;
@@ -335,7 +340,7 @@ extern "C" int nq_count_unique(nq_handle* h, int N, uint64_t* unique, uint64_t* 
       int per = 0;
       if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, unique_kernel<B>, B, smem) != cudaSuccess || per <= 0) { status = NQ_ECUDA; break; }
       UArgs a;
-      a.tasks = (const UTask*)d_tasks; a.confs = (const UConf*)d_confs; a.m = m; a.N = N;
+      a.tasks = (const UTask*)d_tasks; a.confs = (const UConf*)d_confs; a.m = m; a.N = N; a.maxf = maxf;
       a.counts = (unsigned long long*)d_ctl; a.cursor = (unsigned int*)((char*)d_ctl + 32);
       a.err = (unsigned int*)((char*)d_ctl + 36);
       unique_kernel<B><<<sms * per, B, smem, st>>>(a);
