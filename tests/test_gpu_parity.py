@@ -74,6 +74,21 @@ def test_total_n21_largest_configured_board(eng, oracle_mod):
     assert eng.last_run_info()[0] == 1
 
 
+@pytest.mark.parametrize("N", [22, 24])
+def test_large_board_sample_per_record(eng, oracle_mod, N):
+    """A seeded sample of the N=22 and N=24 task lists (preset 7), per record against the oracle; N=24 runs
+    the kernel form with u64 per-task counters."""
+    import nqueens
+    recs = nqueens.gen_records(N)
+    idx = np.sort(np.random.default_rng(N).choice(len(recs), size=48, replace=False))
+    sub = np.ascontiguousarray(recs[idx])
+    del recs
+    total, sol = eng.exec_records(N, sub, want_solutions=True)
+    want = oracle_mod.exec_solutions(N, _o_records(oracle_mod, sub), threads=0)
+    assert np.array_equal(sol, want)
+    assert total == int(want.sum()) > 0
+
+
 def test_reference_dict_dropin(eng, oracle_mod):
     import nqueens
     _, _, cs, _ = nqueens.gen_constellations(11, set(), set(), [], 5)
