@@ -173,16 +173,21 @@ def reference_arm(args):
     return 0
 
 
-def read_traffic():
-    """dram bytes per dfs_kernel launch from the committed ncu summary, or None."""
+def read_profile_figure(key):
+    """A per-launch figure of the dfs_kernel N=19 ncu capture (profiles/dfs_kernel_n19_traffic.txt), or None."""
     p = os.path.join(REPO, "profiles", "dfs_kernel_n19_traffic.txt")
     try:
         for line in open(p):
-            if line.startswith("dram_bytes_per_launch:"):
+            if line.startswith(key + ":"):
                 return float(line.split(":", 1)[1])
     except OSError:
         pass
     return None
+
+
+def read_traffic():
+    """dram bytes per dfs_kernel launch from the committed ncu summary, or None."""
+    return read_profile_figure("dram_bytes_per_launch")
 
 
 def ours_arm(args):
@@ -269,6 +274,18 @@ def ours_arm(args):
     dfs_avg = statistics.mean(dfs_ms)
     achieved_ops = nodes * OPS_PER_NODE / (dfs_avg * 1e-3)
     traffic = read_traffic()
+    # Executed instructions against the issue limit (one warp instruction per clock per SM sub-partition):
+    # the step is issue/math-pipe bound, so this is the fraction that measures the kernel.
+    warp_instr = read_profile_figure("warp_instructions_per_launch")
+    sm_count = torch.cuda.get_device_properties(dev).multi_processor_count
+    issue = None
+    if warp_instr and clk.get("sm_mhz"):
+        peak_wi = sm_count * 4 * clk["sm_mhz"] * 1e6
+        got_wi = warp_instr / (dfs_avg * 1e-3)
+        issue = {"warp_instructions_per_launch": warp_instr, "achieved": got_wi / 1e9, "peak": peak_wi / 1e9,
+                 "unit": "G warp-instr/s", "frac": got_wi / peak_wi,
+                 "source": "instruction count of one ncu capture (profiles/dfs_kernel_n19.md), time of this run, "
+                           "peak = SMs x 4 issue slots x median sampled SM clock"}
     line = {
         "metric": METRIC, "value": value, "unit": "nodes/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -287,7 +304,7 @@ def ours_arm(args):
                      "frac": achieved_ops / int_peak, "traffic": traffic,
                      "peak_source": "measured in this run: lop3.b32 throughput probe (nq_int32_peak); "
                                     f"add.u32 probe {int_peak_add / 1e9:.0f} Gop/s",
-                     "ops_per_node": OPS_PER_NODE,
+                     "ops_per_node": OPS_PER_NODE, "issue": issue,
                      "hbm_frac": (m * 16 + m * 16 + m * 8 + m * 4 * 15) / (dfs_avg * 1e-3) / (
                          (peaks or {}).get("hbm_gbs", 6800.0) * 1e9)},
         "clocks": clk,

@@ -20,3 +20,10 @@ def test_frozen_node_counts(oracle_mod, N):
     rec = oracle_mod.gen_constellations(N, oracle_mod.preset_for(N))
     _, nodes = oracle_mod.exec_solutions(N, rec, want_nodes=True)
     assert int(nodes.sum()) == b.DFS_NODES[N]
+
+
+def test_profile_figures_readable():
+    b = _bench()
+    assert b.read_traffic() > 0
+    assert b.read_profile_figure("warp_instructions_per_launch") > 1e9
+    assert b.read_profile_figure("no_such_figure") is None
