@@ -17,15 +17,16 @@
 //   ncol = col | bit
 //   nf   = bm & ~(nld | nrd | ncol)
 //   FC:   drop the child when bm & ~((nld<<1)|(nrd>>1)|ncol) == 0 (look-ahead,
-//         356Py:1935-1965)
+//         356Py:1935-1965; see extend_lookahead for where it applies)
 //   TERM: the child is a base frame (356Py:1855-1860): count it instead of
-//         descending; B14: base of SQd2B counts only when nf & ~1 != 0;
+//         descending (for SQd2B, whose base counts only when a square other
+//         than column 0 is free, the word's LA carries bit 0);
 //         TALL: count every candidate (completion queries, last free row)
 //
 // Compact word (4 B, single-N plain path):
-//   bits 0-1 LA | bits 2-24 RA | 25 FC | 26 TERM | 27 B14 | 28 TALL | 29-31 s
+//   bits 0-1 LA | bits 2-24 RA | 25 FC | 26 TERM | 28 TALL | 29-31 s
 // Wide word (8 B, mixed batches and completion queries):
-//   x: bits 0-23 LA | 24-26 s | 27 FC | 28 TERM | 29 B14 | 30 TALL;  y: RA
+//   x: bits 0-23 LA | 24-26 s | 27 FC | 28 TERM | 30 TALL;  y: RA
 #pragma once
 #include <stdint.h>
 
@@ -45,7 +46,6 @@ constexpr uint32_t C_LA = 0x3u;
 constexpr uint32_t C_RA = 0x01FFFFFCu;
 constexpr uint32_t C_FC = 1u << 25;
 constexpr uint32_t C_TERM = 1u << 26;
-constexpr uint32_t C_B14 = 1u << 27;
 constexpr uint32_t C_TALL = 1u << 28;
 constexpr int C_SSHIFT = 29;   // s in 1..3: walk_schedule steps 1, 2 or 3 rows (the DFS forms 1 << s as s*s - s + 2)
 // wide word fields (x)
@@ -53,7 +53,6 @@ constexpr uint32_t W_LA = 0x00FFFFFFu;
 constexpr int W_SSHIFT = 24;
 constexpr uint32_t W_FC = 1u << 27;
 constexpr uint32_t W_TERM = 1u << 28;
-constexpr uint32_t W_B14 = 1u << 29;
 constexpr uint32_t W_TALL = 1u << 30;
 
 // Task info word: T (terminal depth, 0..31) | wexp<<5 | root_count<<7 | N<<8 |
@@ -190,7 +189,7 @@ NQ_HD TaskHead decode_record(int N, uint32_t rld, uint32_t rrd, uint32_t rcol, u
 }
 
 // One schedule entry before packing.
-struct Op { uint32_t s, la, ra, fc, term, b14, tall; };
+struct Op { uint32_t s, la, ra, fc, term, tall; };
 
 // Look-ahead wherever it is sound, not only where the reference applies it
 // (fr.av == 1 frames).  A word's look-ahead prunes the child frame when the
@@ -229,7 +228,6 @@ NQ_HD int walk_schedule(int N, const TaskHead& t, Root* root, uint32_t* root_cou
         return -1;
       }
       ops[d - 1].term = 1;
-      ops[d - 1].b14 = (fid == 14);
       // The terminal-parent frame never descends, so its LA bits only feed the
       // child row's free set: LA bit 0 there removes column 0, which is the
       // SQd2B base rule "count only if a square other than column 0 is free"
@@ -239,7 +237,7 @@ NQ_HD int walk_schedule(int N, const TaskHead& t, Root* root, uint32_t* root_cou
       return d - 1;
     }
     if (d >= max_depth || row > 31) return -2;
-    Op op = {1, 0, 0, 0, 0, 0, 0};
+    Op op = {1, 0, 0, 0, 0, 0};
     int nfid = fid;
     bool at_mark = false;
     if (fr.ptn <= 2) at_mark = (fr.ptn == 1) ? (row == t.mark2) : (row == t.mark1);
@@ -265,11 +263,11 @@ NQ_HD int walk_schedule(int N, const TaskHead& t, Root* root, uint32_t* root_cou
 }
 
 NQ_HD uint32_t pack_compact(const Op& o) {
-  return (o.la & C_LA) | (o.ra & C_RA) | (o.fc ? C_FC : 0u) | (o.term ? C_TERM : 0u) | (o.b14 ? C_B14 : 0u) |
+  return (o.la & C_LA) | (o.ra & C_RA) | (o.fc ? C_FC : 0u) | (o.term ? C_TERM : 0u) |
          (o.tall ? C_TALL : 0u) | (o.s << C_SSHIFT);
 }
 NQ_HD uint32_t pack_wide_x(const Op& o) {
-  return (o.la & W_LA) | (o.s << W_SSHIFT) | (o.fc ? W_FC : 0u) | (o.term ? W_TERM : 0u) | (o.b14 ? W_B14 : 0u) |
+  return (o.la & W_LA) | (o.s << W_SSHIFT) | (o.fc ? W_FC : 0u) | (o.term ? W_TERM : 0u) |
          (o.tall ? W_TALL : 0u);
 }
 

@@ -226,7 +226,7 @@ int build_completion_tasks(int N, int k, const int* rows, const int* cols, int m
   uint32_t ld = 0, rd = 0, col = 0;
   Op ops[kMaxDepth + 1];
   if (n > kMaxDepth) return -1;
-  for (int d = 0; d < n; d++) ops[d] = Op{1, 0, 0, 0, 0, 0, 0};
+  for (int d = 0; d < n; d++) ops[d] = Op{1, 0, 0, 0, 0, 0};
   for (int q = 0; q < k; q++) {
     const int r = rows[q], c = cols[q];
     col |= 1u << c;

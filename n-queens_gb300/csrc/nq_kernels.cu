@@ -121,18 +121,18 @@ cudaError_t launch_prepare(int N, int64_t m, const uint4* records, const TaskArr
 // ---------------------------------------------------------------------------
 // Schedule word decoding shared by the split and DFS kernels
 // ---------------------------------------------------------------------------
-struct Dec { uint32_t s, la, ra, fc, term, b14, tall; };
+struct Dec { uint32_t s, la, ra, fc, term, tall; };
 __device__ __forceinline__ Dec decode(uint32_t w) {
-  return Dec{w >> C_SSHIFT, w & C_LA, w & C_RA, w & C_FC, w & C_TERM, w & C_B14, w & C_TALL};
+  return Dec{w >> C_SSHIFT, w & C_LA, w & C_RA, w & C_FC, w & C_TERM, w & C_TALL};
 }
 __device__ __forceinline__ Dec decode(uint2 w) {
-  return Dec{(w.x >> W_SSHIFT) & 7u, w.x & W_LA, w.y, w.x & W_FC, w.x & W_TERM, w.x & W_B14, w.x & W_TALL};
+  return Dec{(w.x >> W_SSHIFT) & 7u, w.x & W_LA, w.y, w.x & W_FC, w.x & W_TERM, w.x & W_TALL};
 }
 
 // The same decode with the shift field taken by a multiply-high, which issues
 // on the FMA pipe instead of the integer ALU pipe (the DFS step's binding pipe).
 __device__ __forceinline__ Dec decode_fma(uint32_t w) {
-  return Dec{__umulhi(w, 1u << (32 - C_SSHIFT)), w & C_LA, w & C_RA, w & C_FC, w & C_TERM, w & C_B14, w & C_TALL};
+  return Dec{__umulhi(w, 1u << (32 - C_SSHIFT)), w & C_LA, w & C_RA, w & C_FC, w & C_TERM, w & C_TALL};
 }
 __device__ __forceinline__ Dec decode_fma(uint2 w) { return decode(w); }
 
@@ -204,7 +204,7 @@ __global__ void __launch_bounds__(256) split_kernel(int pass, int64_t t0, int64_
         const uint32_t ncol = f.z | bit;
         uint32_t nf = bm & ~(nld | nrd | ncol);
         if (o.fc && (bm & ~((nld << 1) | (nrd >> 1) | ncol)) == 0u) nf = 0;
-        if (o.term) { direct += ((nf & (o.b14 ? ~1u : ~0u)) != 0u || o.tall) ? 1u : 0u; continue; }
+        if (o.term) { direct += (nf != 0u || o.tall) ? 1u : 0u; continue; }   // SQd2B: LA bit 0
         if (nf == 0u) continue;
         if (k + 1 == D) {
           if (pass == 1) {

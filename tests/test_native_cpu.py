@@ -114,20 +114,19 @@ def replay(root, info, words, wide):
         if wide:
             x, ra = words[d]
             s = (x >> 24) & 7; la = x & 0xFFFFFF
-            fc, term, b14, tall = x & (1 << 27), x & (1 << 28), x & (1 << 29), x & (1 << 30)
+            fc, term, tall = x & (1 << 27), x & (1 << 28), x & (1 << 30)
         else:
             w = words[d]
             s = w >> 29; la = w & 3; ra = w & 0x01FFFFFC
-            fc, term, b14, tall = w & (1 << 25), w & (1 << 26), w & (1 << 27), w & (1 << 28)
+            fc, term, tall = w & (1 << 25), w & (1 << 26), w & (1 << 28)
         nld = (((ld | bit) << s) & M32) | la
         nrd = ((rd | bit) >> s) | ra
         ncol = col | bit
         nf = bm & ~(nld | nrd | ncol)
         if fc and (bm & ~((((nld << 1) & M32) | (nrd >> 1) | ncol))) == 0:
             nf = 0
-        if term:
-            tm = (M32 & ~1) if b14 else M32
-            cnt += 1 if ((nf & tm) != 0 or tall) else 0
+        if term:                     # SQd2B: LA bit 0 of the word already removed column 0
+            cnt += 1 if (nf != 0 or tall) else 0
         elif nf:
             if avail:
                 stack.append((ld, rd, col, avail, d))
