@@ -446,10 +446,23 @@ __global__ void __launch_bounds__(BLOCK) dfs_kernel(const DfsArgs a) {
   }
 }
 
+// The dynamic shared-memory cap of a kernel is one process-wide attribute.
+// It is always set to the device's opt-in maximum, never to one launch's
+// size: a smaller launch (a per-job run, an occupancy query) must not lower
+// the cap under a larger launch captured earlier in a CUDA graph.
+template <typename K>
+cudaError_t allow_max_dynamic_smem(K kernel) {
+  int dev = 0, optin = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+  return e;
+}
+
 template <bool WIDE, int BLOCK, bool BIG>
 static cudaError_t launch_dfs_t(const DfsLaunch& L, cudaStream_t st) {
   const size_t smem = dfs_smem_bytes(WIDE, BLOCK, L.maxt);
-  cudaError_t e = cudaFuncSetAttribute(dfs_kernel<WIDE, BLOCK, BIG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = allow_max_dynamic_smem(dfs_kernel<WIDE, BLOCK, BIG>);
   if (e != cudaSuccess) return e;
   int grid = L.grid;
   if (grid <= 0) {
@@ -489,9 +502,7 @@ cudaError_t launch_dfs(const DfsLaunch& L, cudaStream_t st) {
 template <bool WIDE, int BLOCK>
 static int occ(int maxt) {
   const size_t smem = dfs_smem_bytes(WIDE, BLOCK, maxt);
-  if (cudaFuncSetAttribute(dfs_kernel<WIDE, BLOCK, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-      cudaSuccess)
-    return 0;
+  if (allow_max_dynamic_smem(dfs_kernel<WIDE, BLOCK, false>) != cudaSuccess) return 0;
   int per = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, dfs_kernel<WIDE, BLOCK, false>, BLOCK, smem) != cudaSuccess)
     return 0;

@@ -336,7 +336,11 @@ extern "C" int nq_count_unique(nq_handle* h, int N, uint64_t* unique, uint64_t* 
     if (m > 0 && cudaMemcpyAsync(d_tasks, tasks.data(), (size_t)m * sizeof(UTask), cudaMemcpyHostToDevice, st) != cudaSuccess) { status = NQ_ECUDA; break; }
     if (!confs.empty() && cudaMemcpyAsync(d_confs, confs.data(), confs.size() * sizeof(UConf), cudaMemcpyHostToDevice, st) != cudaSuccess) { status = NQ_ECUDA; break; }
     if (m > 0) {
-      if (cudaFuncSetAttribute(unique_kernel<B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) { status = NQ_ECUDA; break; }
+      int optin = 0;   // the cap is process-wide: set it to the device maximum, never to one launch's size
+      if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess ||
+          cudaFuncSetAttribute(unique_kernel<B>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) != cudaSuccess) {
+        status = NQ_ECUDA; break;
+      }
       int per = 0;
       if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, unique_kernel<B>, B, smem) != cudaSuccess || per <= 0) { status = NQ_ECUDA; break; }
       UArgs a;
