@@ -368,12 +368,14 @@ def exec_solutions(N: int, constellations: List[Dict[str, int]], use_gpu: bool =
     if not constellations:
         return
     eng = default_engine()
-    _, _, split = eng.get_config()
-    eng.set_config(gpu_block if gpu_block in (64, 128, 256) else 64, max(0, int(gpu_max_blocks)), split)
+    block = gpu_block if gpu_block in (64, 128, 256) else 64
+    if (block, int(gpu_max_blocks)) != (64, 0):      # explicit launch knobs; the defaults keep the tuned table
+        _, _, split = eng.get_config()
+        eng.set_config(block, max(0, int(gpu_max_blocks)), split)
     recs = records_from_constellations(constellations)
     total, sol = eng.exec_records(N, recs, want_solutions=True)
-    for c, v in zip(constellations, sol.tolist()):
-        c["solutions"] = int(v)
+    for c, v in zip(constellations, sol.tolist()):     # tolist() gives Python ints
+        c["solutions"] = v
     if gpu_log_level >= 1:
         print(f"[gpu-summary] N={N} constellations={len(constellations)} total={total}")
 
