@@ -37,7 +37,7 @@ for _p in (os.path.join(REPO, "n-queens_gb300"), os.path.join(REPO, "oracle")):
 # DFS nodes per N at the reference's dynamic preset (select_dynamic_preset_queens), counted by
 # oracle.exec_solutions(N, oracle.gen_constellations(N, preset), want_nodes=True).
 DFS_NODES = {10: 4980, 11: 27032, 12: 145880, 13: 787610, 14: 4578224, 15: 27864613, 16: 182533515,
-             17: 1247485360, 18: 9087554384, 19: 69276398858, 20: 557537122738}
+             17: 1247485360, 18: 9087554384, 19: 69276398858, 20: 557537122738, 21: 4670180074483}
 N_BENCH = 19
 OPS_PER_NODE = 12   # INT32 ops per node in the reference hot loop (neg, and, xor, or, shl, or, shr, or, or, or, andnot, cmp)
 METRIC = "N=19 DFS nodes/s"
