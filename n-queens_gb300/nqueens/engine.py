@@ -20,6 +20,7 @@ CPU.
 from __future__ import annotations
 
 import ctypes
+import os
 from dataclasses import dataclass, field
 from typing import Dict, Iterable, List, Optional, Sequence, Set, Tuple
 
@@ -347,9 +348,17 @@ _default: Optional[Engine] = None
 
 
 def default_engine() -> Engine:
+    """The process's engine: device LOCAL_RANK under a per-GPU launcher (torchrun), device 0 otherwise or
+    when the launcher gives each rank only its own device."""
     global _default
     if _default is None:
-        _default = Engine(0)
+        dev = int(os.environ.get("LOCAL_RANK", "0"))
+        try:
+            _default = Engine(dev)
+        except NQError:
+            if dev == 0:
+                raise
+            _default = Engine(0)
     return _default
 
 
