@@ -134,14 +134,18 @@ int gen_constellations(int N, int preset, std::vector<GenRecord>& out, int threa
   out.clear();
   if (N < 5 || N > kMaxN || preset < 1) return -1;
   const int halfN = (N + 1) / 2, N1 = N - 1, N2 = N - 2;
+  // S: the set of start constellations (random access for the rotation check),
+  // with its members also listed so nothing scans all 2^20 packed ijkl values.
   std::vector<uint8_t> S(1u << 20, 0);
+  std::vector<int> members;
+  auto add = [&](int x) { if (!S[x]) { S[x] = 1; members.push_back(x); } };
   if (N % 2 == 1) {   // centre column of odd boards (356Py:2857-2867)
     const int c = N / 2;
     for (int l = c + 1; l < N1; l++)
       for (int i = c + 1; i < N1; i++) {
         if (i == N1 - l) continue;
         for (int j = N - c - 2; j > 0; j--)
-          if (j != i && j != l && !rotated_present(S, i, j, c, l, N)) S[to_ijkl(i, j, c, l)] = 1;
+          if (j != i && j != l && !rotated_present(S, i, j, c, l, N)) add(to_ijkl(i, j, c, l));
       }
   }
   for (int k = 1; k < halfN; k++)   // no queen in a corner (356Py:2869-2878)
@@ -149,16 +153,16 @@ int gen_constellations(int N, int preset, std::vector<GenRecord>& out, int threa
       for (int i = k + 1; i < N1; i++) {
         if (i == N1 - l) continue;
         for (int j = N - k - 2; j > 0; j--)
-          if (j != i && j != l && !rotated_present(S, i, j, k, l, N)) S[to_ijkl(i, j, k, l)] = 1;
+          if (j != i && j != l && !rotated_present(S, i, j, k, l, N)) add(to_ijkl(i, j, k, l));
       }
   for (int j = 1; j < N2; j++)      // queen in a corner (356Py:2880)
-    for (int l = j + 1; l < N1; l++) S[to_ijkl(0, j, 0, l)] = 1;
-  std::vector<uint8_t> C(1u << 20, 0);
-  for (int x = 0; x < (1 << 20); x++)
-    if (S[x]) C[canon(x, N)] = 1;
+    for (int l = j + 1; l < N1; l++) add(to_ijkl(0, j, 0, l));
+  // canonical forms (jasmin), distinct, in ascending packed order
   std::vector<int> starts;
-  for (int x = 0; x < (1 << 20); x++)
-    if (C[x]) starts.push_back(x);
+  starts.reserve(members.size());
+  for (int x : members) starts.push_back(canon(x, N));
+  std::sort(starts.begin(), starts.end());
+  starts.erase(std::unique(starts.begin(), starts.end()), starts.end());
 
   const size_t ns = starts.size();
   std::vector<std::vector<GenRecord>> parts(ns);
