@@ -268,6 +268,7 @@ int build_unique_tasks(int N, int64_t min_tasks, std::vector<UConf>& confs, std:
   while ((int64_t)cur.size() < min_tasks) {
     bool grew = false;
     nxt.clear();
+    nxt.reserve(cur.size() * (size_t)N);
     for (auto& cs : cur) {
       const UConf& c = confs[cs.first];
       const S& s = cs.second;
@@ -286,6 +287,7 @@ int build_unique_tasks(int N, int64_t min_tasks, std::vector<UConf>& confs, std:
     cur.swap(nxt);
     if (!grew) break;
   }
+  tasks.reserve(tasks.size() + cur.size());
   for (auto& cs : cur) {
     const UConf& c = confs[cs.first];
     const S& s = cs.second;
