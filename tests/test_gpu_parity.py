@@ -74,10 +74,10 @@ def test_total_n21_largest_configured_board(eng, oracle_mod):
     assert eng.last_run_info()[0] == 1
 
 
-@pytest.mark.parametrize("N", [22, 24])
+@pytest.mark.parametrize("N", [20, 21, 22, 24])
 def test_large_board_sample_per_record(eng, oracle_mod, N):
-    """A seeded sample of the N=22 and N=24 task lists (preset 7), per record against the oracle; N=24 runs
-    the kernel form with u64 per-task counters."""
+    """A seeded sample of the N=20, 21 (preset 6), 22 and 24 (preset 7) task lists, per record against the
+    oracle; N=24 runs the kernel form with u64 per-task counters."""
     import nqueens
     recs = nqueens.gen_records(N)
     idx = np.sort(np.random.default_rng(N).choice(len(recs), size=48, replace=False))
