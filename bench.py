@@ -69,7 +69,10 @@ class Clocks:
     def __init__(self, device: int):
         self.device = device
         self.proc = None
-        self.path = os.path.join(REPO, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+        # raw samples; NQ_CLOCKS_DIR keeps them somewhere chosen (default: the temp directory)
+        import tempfile
+        d = os.environ.get("NQ_CLOCKS_DIR") or tempfile.gettempdir()
+        self.path = os.path.join(d, f"clocks_bench_{os.getpid()}.csv")
 
     def start(self):
         try:
