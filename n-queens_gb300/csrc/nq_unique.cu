@@ -235,17 +235,18 @@ __global__ void __launch_bounds__(BLOCK) unique_kernel(const UArgs a) {
 // expanded breadth-first over its first rows until there are enough tasks.
 int build_unique_tasks(int N, int64_t min_tasks, std::vector<UConf>& confs, std::vector<UTask>& tasks) {
   const uint32_t mask = (1u << N) - 1u;
-  struct S { uint32_t left, down, right, row; uint32_t board[kBoardWords]; };
-  std::vector<std::pair<uint32_t, S>> cur;   // (conf, state at row with its candidate set still to take)
+  // Search states are kept in the task layout itself (avail is filled in at the
+  // end), so the last level becomes the task list without another copy.
+  std::vector<UTask> cur;
   // part 1: corner queen
   for (int b1 = 2; b1 < N - 1; b1++) {
     UConf c = {1, (uint32_t)b1, 0, 0, 0, 0, 1u << (N - 1)};
     confs.push_back(c);
     const uint32_t bit = 1u << b1;
-    S s{};
+    UTask s{};
     s.left = (2u | bit) << 1; s.down = 1u | bit; s.right = (2u | bit) >> 1; s.row = 2;
-    s.board[0] = 1; s.board[1] = bit;
-    cur.push_back({(uint32_t)confs.size() - 1, s});
+    s.board[0] = 1; s.board[1] = bit; s.conf = (uint32_t)confs.size() - 1;
+    cur.push_back(s);
   }
   // part 2: no corner queen
   {
@@ -256,47 +257,47 @@ int build_unique_tasks(int N, int64_t min_tasks, std::vector<UConf>& confs, std:
       UConf c = {2, (uint32_t)b1, (uint32_t)b2, endbit, lastmask, sidemask, topbit};
       confs.push_back(c);
       const uint32_t bit = 1u << b1;
-      S s{};
+      UTask s{};
       s.left = bit << 1; s.down = bit; s.right = bit >> 1; s.row = 1; s.board[0] = bit;
-      cur.push_back({(uint32_t)confs.size() - 1, s});
+      s.conf = (uint32_t)confs.size() - 1;
+      cur.push_back(s);
       endbit >>= 1;
       lastmask = (lastmask << 1) | lastmask | (lastmask >> 1);
     }
   }
-  // expand rows breadth-first while the tasks stay above the last row and fit the board prefix
-  std::vector<std::pair<uint32_t, S>> nxt;
+  // expand whole rows breadth-first (tasks of one row are of similar size) while
+  // the tasks stay above the last row and fit the board prefix
+  std::vector<UTask> nxt;
   while ((int64_t)cur.size() < min_tasks) {
     bool grew = false;
     nxt.clear();
     nxt.reserve(cur.size() * (size_t)N);
-    for (auto& cs : cur) {
-      const UConf& c = confs[cs.first];
-      const S& s = cs.second;
-      if ((int)s.row + 1 >= N - 1 || s.row + 1 >= (uint32_t)kBoardWords) { nxt.push_back(cs); continue; }
-      uint32_t bm = row_filter(mask & ~(s.left | s.down | s.right), s.row, s.down, c);
+    for (const UTask& s : cur) {
+      if ((int)s.row + 1 >= N - 1 || s.row + 1 >= (uint32_t)kBoardWords) { nxt.push_back(s); continue; }
+      uint32_t bm = row_filter(mask & ~(s.left | s.down | s.right), s.row, s.down, confs[s.conf]);
       while (bm) {
         const uint32_t bit = bm & (0u - bm);
         bm ^= bit;
-        S t = s;
+        UTask t = s;
         t.board[s.row] = bit;
         t.left = (s.left | bit) << 1; t.down = s.down | bit; t.right = (s.right | bit) >> 1; t.row = s.row + 1;
-        nxt.push_back({cs.first, t});
+        nxt.push_back(t);
         grew = true;
       }
     }
     cur.swap(nxt);
     if (!grew) break;
   }
-  tasks.reserve(tasks.size() + cur.size());
-  for (auto& cs : cur) {
-    const UConf& c = confs[cs.first];
-    const S& s = cs.second;
-    UTask t{};
-    t.left = s.left; t.down = s.down; t.right = s.right; t.row = s.row; t.conf = cs.first;
-    t.avail = row_filter(mask & ~(s.left | s.down | s.right), s.row, s.down, c);
-    for (int r = 0; r < kBoardWords; r++) t.board[r] = s.board[r];
-    if (t.avail) tasks.push_back(t);
+  // each state's candidate set; states without one are dropped (in place)
+  size_t k = 0;
+  for (size_t q = 0; q < cur.size(); q++) {
+    UTask& t = cur[q];
+    t.avail = row_filter(mask & ~(t.left | t.down | t.right), t.row, t.down, confs[t.conf]);
+    if (t.avail) cur[k++] = t;
   }
+  cur.resize(k);
+  if (tasks.empty()) tasks.swap(cur);
+  else tasks.insert(tasks.end(), cur.begin(), cur.end());
   return 0;
 }
 
