@@ -198,6 +198,16 @@ def test_completions_match_bruteforce(eng, oracle_mod, N):
         assert eng.count_completions(N, q) == want, (N, q)
 
 
+@pytest.mark.parametrize("N", [14, 15, 16, 17])
+def test_completions_larger_boards(eng, oracle_mod, N):
+    """One to eight pre-placed queens on larger boards (seeded rows and columns) against brute force."""
+    rng = np.random.default_rng(700 + N)
+    for k in ((1, 2, 3) if N < 17 else (2, 3)) + (6, 8):
+        q = _queens(rng, N, k)
+        want = oracle_mod.completions(N, [r for r, _ in q], [c for _, c in q])
+        assert eng.count_completions(N, q) == want, (N, q)
+
+
 def test_completion_edge_cases(eng, oracle_mod):
     assert eng.count_completions(8, [(0, 0), (1, 1)]) == 0          # attacking
     assert eng.count_completions(8, [(3, 3), (3, 5)]) == 0          # two queens in one row
