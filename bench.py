@@ -246,6 +246,8 @@ def ours_arm(args):
         assert int(d_total.item()) == expected
     split_depth, queued = eng.last_run_info()
     torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
     clk = clocks.stop()
     step_ms = [a.elapsed_time(b) for a, b in ev]
     t_ms = sum(step_ms)
