@@ -113,6 +113,14 @@ int nq_last_run_info(const nq_handle *h, int *split_depth, int64_t *queued);
 int nq_exec_solutions_noalloc(int N, const nq_record *d_records, int64_t m, int start_min, uint64_t *d_solutions,
                               uint64_t *d_total, void *stream);
 
+/* Autotuner: times the whole count of N (its default preset's task list,
+ * resident on the device) for every threads-per-block (64/128/256) and split
+ * depth (0..3), `repeats` timed runs each after one warm-up, checks that every
+ * configuration gives the same total, leaves the fastest set on the handle and
+ * reports it.  Replaces hand-setting the reference's launch knobs
+ * (gpu_block / gpu_max_blocks of exec_solutions, 356Py_savesp_narrow.py:2228). */
+int nq_tune(nq_handle *h, int N, int repeats, int *best_block, int *best_split, float *best_ms);
+
 /* Whole-board total for N, the loop body of the reference's main()
  * (356Py_savesp_narrow.py:6036-6046): brute force on the GPU for N <= 5
  * (the reference's _bit_total, :5755-5767), the constellation path above.

@@ -485,6 +485,52 @@ int64_t nq_debug_completion_tasks(int N, int k, const int* rows, const int* cols
 
 int nq_count_completions(nq_handle* h, int N, int k, const int* rows, const int* cols, uint64_t* count);
 
+int nq_tune(nq_handle* h, int N, int repeats, int* best_block, int* best_split, float* best_ms) {
+  if (!h || repeats < 1) return h ? h->fail(NQ_EINVAL, "tune: bad arguments") : NQ_EINVAL;
+  if (N < 6 || N > kMaxN) return h->fail(NQ_EINVAL, "tune: N=%d outside 6..27", N);
+  std::vector<GenRecord> v;
+  const int g = gen_constellations(N, preset_for(N), v, 0);
+  if (g != 0) return h->fail(g == -2 ? NQ_EPRESET : NQ_EINVAL, "tune: generator failed for N=%d", N);
+  const int64_t m = (int64_t)v.size();
+  if (m == 0) return h->fail(NQ_EINVAL, "tune: no tasks for N=%d", N);
+  std::vector<nq_record> r((size_t)m);
+  for (int64_t i = 0; i < m; i++) r[i] = nq_record{(uint32_t)v[i].ld, (uint32_t)v[i].rd, (uint32_t)v[i].col, v[i].startijkl};
+  cudaStream_t st = h->stream;
+  NQ_CUDA(h, cudaSetDevice(h->device));
+  const int smin = (int)start_row_min(&r[0].startijkl, m, 4);
+  NQ_CUDA(h, h->rec.ensure((size_t)m * sizeof(nq_record)));
+  NQ_CUDA(h, cudaMemcpyAsync(h->rec.p, r.data(), (size_t)m * sizeof(nq_record), cudaMemcpyHostToDevice, st));
+  const int old_block = h->block, old_split = h->split;
+  float best = 1e30f;
+  int bb = old_block, bs = old_split;
+  uint64_t want = 0;
+  bool have_total = false;
+  for (int b : {64, 128, 256})
+    for (int s = 0; s <= 3; s++) {
+      h->block = b; h->split = s;
+      for (int k = 0; k <= repeats; k++) {           // first run warms up, then `repeats` timed runs
+        uint64_t total = 0;
+        int st_run = run_records(h, N, (const uint4*)h->rec.p, m, smin, nullptr, st);
+        if (st_run == NQ_OK) st_run = read_ctrl(h, st, &total);
+        if (st_run != NQ_OK) { h->block = old_block; h->split = old_split; return st_run; }
+        if (!have_total) { want = total; have_total = true; }
+        if (total != want) {
+          h->block = old_block; h->split = old_split;
+          return h->fail(NQ_ECUDA, "tune: N=%d count changed between configurations", N);
+        }
+        if (k == 0) continue;
+        float ms = 0.f;
+        NQ_CUDA(h, cudaEventElapsedTime(&ms, h->ev[0], h->ev[2]));
+        if (ms < best) { best = ms; bb = b; bs = s; }
+      }
+    }
+  h->block = bb; h->split = bs;                       // the handle keeps the fastest configuration
+  if (best_block) *best_block = bb;
+  if (best_split) *best_split = bs;
+  if (best_ms) *best_ms = best;
+  return NQ_OK;
+}
+
 int nq_count(nq_handle* h, int N, int preset, uint64_t* total) {
   if (!h || !total) return NQ_EINVAL;
   if (N < 1 || N > kMaxN) return h->fail(NQ_EINVAL, "N=%d outside 1..27", N);

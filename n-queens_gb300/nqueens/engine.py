@@ -247,6 +247,15 @@ class Engine:
         _check(lib().nq_set_config(self._h, block, grid, split), self._h, "set_config")
         self._tuning = None
 
+    def tune_native(self, N: int, repeats: int = 2) -> Tuple[int, int, float]:
+        """The C ABI's autotuner (nq_tune): (block, split depth, best ms); the handle keeps that configuration
+        (and the per-N table is switched off, as with set_config)."""
+        b, s, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_float()
+        _check(lib().nq_tune(self._h, int(N), int(repeats), ctypes.byref(b), ctypes.byref(s), ctypes.byref(ms)),
+               self._h, f"tune(N={N})")
+        self._tuning = None
+        return b.value, s.value, ms.value
+
     def get_config(self) -> Tuple[int, int, int]:
         b, g, o = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         _check(lib().nq_get_config(self._h, ctypes.byref(b), ctypes.byref(g), ctypes.byref(o)), self._h)

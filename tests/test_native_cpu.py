@@ -288,3 +288,15 @@ def test_exec_solutions_rejects_cpu_path(nq):
     with pytest.raises(ValueError):
         nq.exec_solutions(8, [{"ld": 0, "rd": 0, "col": 0, "startijkl": 0, "solutions": 0}], use_gpu=False)
 
+
+
+def test_entry_points_reject_a_null_handle(nq):
+    """Calls that need a handle return NQ_EINVAL for a null one (no device is touched)."""
+    import ctypes
+    from nqueens import _lib
+    L = _lib.lib()
+    b, s, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_float()
+    assert L.nq_tune(None, 15, 1, ctypes.byref(b), ctypes.byref(s), ctypes.byref(ms)) == _lib.NQ_EINVAL
+    t = np.zeros(1, np.uint64)
+    assert L.nq_count(None, 10, 0, _lib.p64(t)) == _lib.NQ_EINVAL
+    assert L.nq_set_config(None, 64, 0, -1) == _lib.NQ_EINVAL

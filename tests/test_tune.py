@@ -40,3 +40,17 @@ def test_untuned_n_uses_defaults_not_previous_n(oracle_mod):
         assert eng.get_config() == (64, 0, -1)
     finally:
         eng.close()
+
+
+def test_native_tuner_keeps_fastest_config_and_counts_stay_exact(oracle_mod):
+    import nqueens
+    eng = nqueens.Engine(0)
+    try:
+        b, s, ms = eng.tune_native(15, repeats=1)
+        assert b in (64, 128, 256) and 0 <= s <= 3 and ms > 0
+        assert eng.get_config() == (b, 0, s)
+        assert eng.count(15).total == oracle_mod.EXPECTED_TOTAL[15]
+        with pytest.raises(nqueens.NQError):
+            eng.tune_native(5)                                 # the constellation path starts at N=6
+    finally:
+        eng.close()
