@@ -80,10 +80,11 @@ int nq_exec_solutions(nq_handle *h, int N, const nq_record *records, int64_t m, 
 
 /* Same on device-resident buffers on `stream` (NULL: the handle's stream).
  * `start_min` is the smallest start row (startijkl >> 20) over the records,
- * or -1 to use the bound 1.  d_total (device, 1 x u64) is overwritten.  When
- * the queue is split the call waits once for an 8-byte subtask count before
- * launching the DFS; otherwise it returns after enqueueing.  Call nq_sync()
- * to wait for the result and collect the status. */
+ * or -1 to use the bound 1.  d_total (device, 1 x u64) is overwritten.  The
+ * call waits once for a 40-byte read-back (the subtask count and the deepest
+ * schedule, which size the DFS queue and stacks) before launching the DFS,
+ * then returns.  Call nq_sync() to wait for the result and collect the
+ * status. */
 int nq_exec_solutions_device(nq_handle *h, int N, const nq_record *d_records, int64_t m, int start_min,
                              uint64_t *d_solutions, uint64_t *d_total, void *stream);
 int nq_sync(nq_handle *h);
