@@ -106,10 +106,10 @@ class Server:
                  poll_us: int = 200, share_gpu: bool = True, large_ms: float = 50.0, large_share: float = 0.875):
         self.engine = engine or Engine(device)
         # Lanes: requests estimated above large_ms run one per batch on large_share of the
-        # resident blocks; the rest are batched on the remaining share (share_gpu), so a
-        # small request admitted while a large one runs starts at once beside it.  Shares
-        # are taken of each batch's own resident capacity (its stack depth sets how many
-        # blocks fit on an SM).
+        # resident blocks; the rest are batched on the remaining share while a large batch
+        # runs (share_gpu), so a small request admitted then starts at once beside it, and on
+        # the whole GPU otherwise.  Shares are taken of each batch's own resident capacity
+        # (its stack depth sets how many blocks fit on an SM).
         self.share_gpu = bool(share_gpu)
         self.large_share = float(large_share)
         self.large_ms = float(large_ms)
@@ -238,7 +238,11 @@ class Server:
             return True
         nbytes = batch.device_bytes
         if self.share_gpu:
-            share = self.large_share if large else 1.0 - self.large_share
+            # small batches take the whole GPU while no large batch runs (they end in
+            # milliseconds); beside a large batch they get the small lane's share
+            with self._cv:
+                large_running = any(f.large for f in self._inflight)
+            share = self.large_share if large else (1.0 - self.large_share if large_running else 1.0)
             batch.set_grid(max(1, int(round(batch.resident_blocks() * share))))
         batch.submit(self.use_graph)
         t_built = time.perf_counter()

@@ -86,13 +86,19 @@ def test_results_in_submission_order(fake, oracle_mod):
 
 
 def test_large_requests_get_a_batch_each_and_the_large_share(fake):
+    fake.delay_s = 0.3
     jobs = [nqueens.CountJob(20), nqueens.CountJob(8), nqueens.CountJob(19), nqueens.CountJob(9)]
     _serve(jobs, large_ms=50.0, large_share=0.75)
     large = [b for b in fake.created if any(isinstance(j, nqueens.CountJob) and j.N >= 19 for j in b.jobs)]
     assert len(large) == 2 and all(len(b.jobs) == 1 for b in large)
     assert all(b.grid == 912 for b in large)                       # 0.75 of 1216 resident blocks
     small = [b for b in fake.created if b not in large]
-    assert small and all(b.grid == 304 for b in small)             # the other 0.25
+    assert small and all(b.grid == 304 for b in small)             # the other 0.25, beside a large batch
+
+
+def test_small_batches_take_the_whole_gpu_when_no_large_batch_runs(fake):
+    _serve([nqueens.CountJob(8), nqueens.CountJob(9)], large_ms=50.0, large_share=0.75)
+    assert fake.created and all(b.grid == 1216 for b in fake.created)
 
 
 def test_budget_holds_batches_until_memory_returns(fake):
