@@ -450,7 +450,8 @@ def serve_arm(args):
             "plain": {"jobs_per_s": len(jobs) / span_plain, "p50_ms": 1e3 * float(np.percentile(pl, 50)),
                       "p90_ms": 1e3 * float(np.percentile(pl, 90)), "p99_ms": 1e3 * float(np.percentile(pl, 99)),
                       "max_ms": 1e3 * float(pl.max())},
-            "e2e": {"value": st.jobs_per_s, "unit": "jobs/s", "h2d_bytes_per_step": None, "d2h_bytes_per_step": None},
+            "e2e": {"value": st.jobs_per_s, "unit": "jobs/s", "h2d_bytes_per_step": st.h2d_bytes,
+                    "d2h_bytes_per_step": st.d2h_bytes},
             "exact": True}
     print(json.dumps(line))
     return 0

@@ -183,7 +183,10 @@ int nq_resident_blocks(nq_handle *h, int wide, int maxt, int *blocks);
  * size, schedule word and stack depth): the unit nq_batch_set_grid shares out.
  * No counterpart in the reference (it runs one N per process). */
 int nq_batch_resident_blocks(const nq_batch *b, int *blocks);
+/* Device bytes the batch holds, and host-to-device bytes its build copied
+ * (records of count jobs, tasks of completion jobs). */
 int64_t nq_batch_device_bytes(const nq_batch *b);
+int64_t nq_batch_h2d_bytes(const nq_batch *b);
 /* All jobs in one persistent launch (use_graph: replay a captured CUDA graph). */
 int nq_batch_run(nq_batch *b, int use_graph, uint64_t *totals);
 /* One launch and one read-back per job (the plain form, for comparison). */

@@ -569,6 +569,7 @@ struct nq_batch {
   cudaGraphExec_t graph = nullptr;
   bool submitted = false;
   int64_t device_bytes = 0;
+  int64_t h2d_bytes = 0;                   // host->device bytes of the build (records, host-built tasks)
   cudaError_t set_ordered() {
     for (DevBuf* d : {&rec, &root, &info, &sched, &ctrl, &nsub, &sroot, &sinfo}) d->ordered = stream;
     return cudaSuccess;
@@ -746,6 +747,8 @@ int nq_batch_create(nq_handle* h, const nq_job* jobs, int njobs, nq_batch** out)
     if ((e = jt.ensure((size_t)njobs * sizeof(uint32_t))) != cudaSuccess) break;
     if ((e = cudaMemsetAsync(jt.p, 0, (size_t)njobs * sizeof(uint32_t), st)) != cudaSuccess) break;
     if (m_rec && (e = cudaMemcpyAsync(b->rec.p, recs.data(), (size_t)m_rec * sizeof(nq_record), cudaMemcpyHostToDevice, st)) != cudaSuccess) break;
+    b->h2d_bytes = m_rec * (int64_t)sizeof(nq_record) +
+                   m_host * (int64_t)(sizeof(uint4) + sizeof(uint2) + (size_t)b->sw * sizeof(uint2));
     for (auto& sg : segs)
       if ((e = launch_prepare(sg.N, sg.m, (const uint4*)b->rec.p + sg.rec_off, ta, sg.rec_off, (uint32_t)sg.job, derr, st,
                               (unsigned int*)jt.p + sg.job)) != cudaSuccess) break;
@@ -846,6 +849,7 @@ int nq_batch_resident_blocks(const nq_batch* b, int* blocks) {
 
 int64_t nq_batch_tasks(const nq_batch* b) { return b ? b->m : NQ_EINVAL; }
 int64_t nq_batch_device_bytes(const nq_batch* b) { return b ? b->device_bytes : NQ_EINVAL; }
+int64_t nq_batch_h2d_bytes(const nq_batch* b) { return b ? b->h2d_bytes : NQ_EINVAL; }
 
 int nq_batch_submit(nq_batch* b, int use_graph) {
   if (!b) return NQ_EINVAL;

@@ -88,6 +88,7 @@ SIGNATURES = {
     "nq_batch_resident_blocks": (ctypes.c_int, [_vp, _ip]),
     "nq_tune": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _ip, _ip, ctypes.POINTER(ctypes.c_float)]),
     "nq_batch_device_bytes": (ctypes.c_int64, [_vp]),
+    "nq_batch_h2d_bytes": (ctypes.c_int64, [_vp]),
     "nq_batch_run": (ctypes.c_int, [_vp, ctypes.c_int, _u64p]),
     "nq_batch_run_plain": (ctypes.c_int, [_vp, _u64p]),
     "nq_batch_submit": (ctypes.c_int, [_vp, ctypes.c_int]),

@@ -168,6 +168,11 @@ class Batch:
     def device_bytes(self) -> int:
         return int(lib().nq_batch_device_bytes(self._b))
 
+    @property
+    def h2d_bytes(self) -> int:
+        """Host-to-device bytes copied when the batch was built."""
+        return int(lib().nq_batch_h2d_bytes(self._b))
+
     def resident_blocks(self) -> int:
         """DFS blocks resident on the whole GPU for this batch's launch (what set_grid shares out)."""
         v = ctypes.c_int()

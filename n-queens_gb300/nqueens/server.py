@@ -86,6 +86,8 @@ class ServerStats:
     latencies_s: List[float] = field(default_factory=list)
     latencies_by_request: List[float] = field(default_factory=list)   # in submission order
     phases_by_request: List[tuple] = field(default_factory=list)      # (queued, build, run) seconds
+    h2d_bytes: int = 0              # copied to the device by every batch's build
+    d2h_bytes: int = 0              # per-job totals read back
     makespan_s: float = 0.0
     batches: int = 0
     max_inflight_seen: int = 0
@@ -123,6 +125,7 @@ class Server:
         self._inflight: List[_InFlight] = []
         self._building = 0
         self._seq = 0
+        self._h2d = 0
         self._admitted = 0
         self._cv = threading.Condition()
         self._stop = False
@@ -171,7 +174,9 @@ class Server:
             by_req = [r.t_done - r.t_arrival for r in done]
             phases = [(r.t_admit - r.t_arrival, r.t_built - r.t_admit, r.t_done - r.t_built) for r in done]
             span = (self._t_last - self._t0) if self._t0 is not None else 0.0
-            return ServerStats(len(self._done), lat, by_req, phases, span, self._batches, self._max_inflight_seen)
+            return ServerStats(completed=len(self._done), latencies_s=lat, latencies_by_request=by_req,
+                               phases_by_request=phases, h2d_bytes=self._h2d, d2h_bytes=8 * len(self._done),
+                               makespan_s=span, batches=self._batches, max_inflight_seen=self._max_inflight_seen)
 
     def close(self) -> None:
         with self._cv:
@@ -237,6 +242,7 @@ class Server:
                 self._cv.notify_all()
             return True
         nbytes = batch.device_bytes
+        h2d = getattr(batch, "h2d_bytes", 0)
         if self.share_gpu:
             # small batches take the whole GPU while no large batch runs (they end in
             # milliseconds); beside a large batch they get the small lane's share
@@ -250,6 +256,7 @@ class Server:
             r.t_built = t_built
         with self._cv:
             self._inflight.append(_InFlight(batch, take, nbytes, large))
+            self._h2d += h2d
             self._building -= 1
             self._admitted += nbytes
             self._batches += 1

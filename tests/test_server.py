@@ -74,6 +74,7 @@ def test_batch_resident_blocks_and_shared_grid():
     try:
         b = eng.batch([nqueens.CountJob(14), nqueens.CountJob(12), nqueens.CompletionJob(11, [(0, 3)])])
         full = b.resident_blocks()
+        assert b.h2d_bytes >= 16 * 2 and b.device_bytes > b.h2d_bytes
         assert full >= eng.resident_blocks(True, 18) > 0
         want = b.run(use_graph=False)
         b.set_grid(max(1, full // 8))

@@ -29,6 +29,7 @@ class FakeBatch:
                 raise NQError(-1, "batch job: bad pre-placed queens")
         self.jobs = list(jobs)
         self.device_bytes = FakeBatch.bytes_per_job * len(jobs)
+        self.h2d_bytes = 16 * len(jobs)
         self.grid = None
         self.t_submit = None
         self.answers = []
@@ -82,6 +83,7 @@ def test_results_in_submission_order(fake, oracle_mod):
             oracle_mod.completions(j.N, [r for r, _ in j.queens], [c for _, c in j.queens]) for j in jobs]
     assert got == want
     assert st.completed == len(jobs) and len(st.latencies_by_request) == len(jobs)
+    assert st.h2d_bytes == 16 * len(jobs) and st.d2h_bytes == 8 * len(jobs)
     assert all(len(b.jobs) <= 5 for b in fake.created)
 
 
