@@ -381,7 +381,7 @@ def batch_arm(args):
             "speedup_vs_plain_resident": p / g,
             "batch_build_s": build_s, "e2e": {"value": len(Ns) / (build_s + g), "unit": "jobs/s",
                                               "seconds_per_step": build_s + g,
-                                              "h2d_bytes_per_step": 16 * b.tasks, "d2h_bytes_per_step": 8 * len(Ns)},
+                                              "h2d_bytes_per_step": b.h2d_bytes, "d2h_bytes_per_step": 8 * len(Ns)},
             "plain_dropin_jobs_per_s": len(Ns) / dropin_s, "speedup_e2e_vs_dropin": dropin_s / (build_s + g),
             "small_mix": small, "gpu_launches": 1}
     b.close()
