@@ -310,6 +310,8 @@ def ours_arm(args):
                      "peak_source": "measured in this run: lop3.b32 throughput probe (nq_int32_peak); "
                                     f"add.u32 probe {int_peak_add / 1e9:.0f} Gop/s",
                      "ops_per_node": OPS_PER_NODE, "issue": issue,
+                     "alu_pipe_pct_of_peak_ncu": read_profile_figure("alu_pipe_pct_of_peak"),
+                     "issue_active_pct_ncu": read_profile_figure("issue_active_pct"),
                      "hbm_frac": (m * 16 + m * 16 + m * 8 + m * 4 * 15) / (dfs_avg * 1e-3) / (
                          (peaks or {}).get("hbm_gbs", 6800.0) * 1e9)},
         "clocks": clk,

@@ -26,4 +26,5 @@ def test_profile_figures_readable():
     b = _bench()
     assert b.read_traffic() > 0
     assert b.read_profile_figure("warp_instructions_per_launch") > 1e9
+    assert 0 < b.read_profile_figure("alu_pipe_pct_of_peak") <= 100
     assert b.read_profile_figure("no_such_figure") is None
