@@ -49,7 +49,8 @@ def test_per_record_counts_match_oracle_dynamic_preset(eng, oracle_mod, N):
     assert total == oracle_mod.EXPECTED_TOTAL[N]
 
 
-@pytest.mark.parametrize("N,preset", [(10, 4), (11, 6), (12, 7), (13, 4), (14, 6), (9, 7), (8, 6)])
+@pytest.mark.parametrize("N,preset", [(10, 4), (11, 6), (12, 7), (13, 4), (14, 6), (9, 7), (8, 6),
+                                      (16, 4), (16, 6), (17, 7), (18, 5)])
 def test_other_presets_match_oracle(eng, oracle_mod, N, preset):
     import nqueens
     recs = nqueens.gen_records(N, preset)
