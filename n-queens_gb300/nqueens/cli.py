@@ -1,6 +1,7 @@
 """Command line: the reference's per-N table, on the GB300 engine.
 
     python -m nqueens [nmin nmax] [--repeat R] [--split D] [--block B] [--unique]
+    python -m nqueens --tasks constellations_N19_6.bin [--write-solutions solutions_N19_6_v2.bin]
 
 prints, like the reference's main() (14Bit_codon_GPU/356Py_savesp_narrow.py:5899-6046),
 
@@ -12,6 +13,10 @@ reference's known-answer table (356Py_savesp_narrow.py:5775).  Unique is 0 on
 the constellation path, as in the reference, unless --unique is given.
 --repeat runs each count R times (the last one is printed), which is how
 profiles/ captures a warm kernel.
+
+--tasks counts one of the reference's cached task files (16-byte records,
+N taken from the file name or --n) and --write-solutions writes the
+per-record counts as the reference's 40-byte solutions_*_v2.bin cache.
 """
 from __future__ import annotations
 
@@ -31,6 +36,32 @@ def _fmt(td: dt.timedelta) -> str:
     return str(td)[:-3] if td.microseconds else str(td) + ".000"
 
 
+def _count_task_file(a) -> int:
+    import os
+    import re
+
+    import numpy as np
+
+    from . import formats
+    m = re.search(r"_N(\d+)_", os.path.basename(a.tasks))
+    N = a.n or (int(m.group(1)) if m else 0)
+    if not 6 <= N <= 27:
+        print(f"{a.tasks}: give the board size with --n (6..27)", file=sys.stderr)
+        return 2
+    recs = formats.load_tasks(a.tasks)
+    eng = Engine(a.device, block=a.block, split=a.split)
+    t0 = dt.datetime.now()
+    total, sol = eng.exec_records(N, recs, want_solutions=bool(a.write_solutions))
+    el = dt.datetime.now() - t0
+    status = "ok" if N < len(EXPECTED) and EXPECTED[N] == total else "(no known answer for this task set)"
+    print(f"{a.tasks}: N={N} records={len(recs)} total={total} {_fmt(el)} {status}")
+    if a.write_solutions:
+        formats.save_solutions(a.write_solutions, recs["ld"].astype(np.uint64), recs["rd"].astype(np.uint64),
+                               recs["col"].astype(np.uint64), recs["startijkl"].astype(np.uint64), sol)
+    eng.close()
+    return 0
+
+
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser(prog="python -m nqueens", description=__doc__.split("\n")[0])
     ap.add_argument("nmin", nargs="?", type=int, default=5)
@@ -40,7 +71,12 @@ def main(argv=None) -> int:
     ap.add_argument("--block", type=int, default=64)
     ap.add_argument("--device", type=int, default=0)
     ap.add_argument("--unique", action="store_true", help="also count unique solutions (symmetry method)")
+    ap.add_argument("--tasks", help="count a reference task file constellations_N{N}_{P}.bin")
+    ap.add_argument("--n", type=int, default=0, help="board size of --tasks when its name does not give it")
+    ap.add_argument("--write-solutions", help="with --tasks: write the per-record counts as a v2 solutions file")
     a = ap.parse_args(argv)
+    if a.tasks:
+        return _count_task_file(a)
     eng = Engine(a.device, block=a.block, split=a.split)   # the defaults keep the autotuned table
     print(" N:             Total           Unique         hh:mm:ss.ms")
     rc = 0

@@ -5,7 +5,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import REPO
+from conftest import REPO, gpu_available
 from golden_util import solution_digest, task_digest
 
 GOLDEN = os.path.join(REPO, "tests", "golden")
@@ -77,3 +77,21 @@ def test_corrupt_files_are_rejected(tmp_path):
     with pytest.raises(formats.FormatError):
         formats.load_solutions(q)
 
+
+
+@pytest.mark.gpu
+@pytest.mark.skipif(not gpu_available(), reason="needs a CUDA GPU")
+def test_cli_counts_a_task_file_and_writes_solutions(tmp_path, oracle_mod, capsys):
+    import nqueens
+    from nqueens import cli, formats
+    N = 12
+    recs = nqueens.gen_records(N)
+    tp = str(tmp_path / formats.task_file_name(N, nqueens.select_dynamic_preset_queens(N)))
+    sp = str(tmp_path / "solutions_out_v2.bin")
+    formats.save_tasks(tp, recs)
+    assert cli.main(["--tasks", tp, "--write-solutions", sp]) == 0
+    assert f"total={oracle_mod.EXPECTED_TOTAL[N]}" in capsys.readouterr().out
+    sol = formats.load_solutions(sp)
+    want = oracle_mod.exec_solutions(N, oracle_mod.Records(recs["ld"].astype(np.uint64), recs["rd"].astype(np.uint64),
+                                                           recs["col"].astype(np.uint64), recs["startijkl"].copy()))
+    assert np.array_equal(sol["solutions"], want) and np.array_equal(sol["startijkl"], recs["startijkl"])
