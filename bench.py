@@ -14,9 +14,11 @@ value: inputs resident in HBM, device-timed (CUDA events on the launching
 stream), L2 flushed (256 MiB write) between timed steps.  e2e: the same
 metric through the C ABI call nq_exec_solutions with pinned host records,
 host->device copy and device->host read-back inside the timed region.
+batch / serve: the metric's second half (the 256-job mixed batch and the
+served completion stream, each against one plain launch per job).
 --impl reference: the reference algorithm's CPU implementation on the host
-cores (the C oracle port, all threads) on a bounded seeded sample of the same
-workload.  Multi-GPU: one process per GPU (torchrun), each rank counts the
+cores (the C oracle port, all threads) on the same workload: the full task
+list cut into one strided slice per timed step.  Multi-GPU: one process per GPU (torchrun), each rank counts the
 full N=19 workload (replicas, weak scaling); value = all ranks' nodes / max time.
 """
 from __future__ import annotations
@@ -38,9 +40,22 @@ for _p in (os.path.join(REPO, "n-queens_gb300"), os.path.join(REPO, "oracle")):
 # oracle.exec_solutions(N, oracle.gen_constellations(N, preset), want_nodes=True).
 DFS_NODES = {10: 4980, 11: 27032, 12: 145880, 13: 787610, 14: 4578224, 15: 27864613, 16: 182533515,
              17: 1247485360, 18: 9087554384, 19: 69276398858, 20: 557537122738, 21: 4670180074483}
-N_BENCH = 19
+N_BENCH = 19          # the headline workload; --n selects another board (tests use small ones)
 OPS_PER_NODE = 12   # INT32 ops per node in the reference hot loop (neg, and, xor, or, shl, or, shr, or, or, or, andnot, cmp)
-METRIC = "N=19 DFS nodes/s"
+
+
+def metric(N: int) -> str:
+    return f"N={N} DFS nodes/s"
+
+
+def preset_of(N: int) -> int:
+    import oracle
+    return oracle.preset_for(N)
+
+
+def expected_total(N: int) -> int:
+    import oracle
+    return oracle.EXPECTED_TOTAL[N]
 
 
 def load_peaks():
@@ -111,24 +126,36 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sms)}
 
 
-def cpu_sample(N: int, frac: float, seed: int):
-    """Seeded subset of the N-workload's records for the CPU legs."""
-    import numpy as np
-    import nqueens
+_ORACLE_RECORDS = {}
+
+
+def oracle_records(N: int, preset: int):
+    """The reference's task list for (N, preset), made by the oracle's own generator (no engine code)."""
     import oracle
-    recs = nqueens.gen_records(N)
+    oracle.build()
+    if (N, preset) not in _ORACLE_RECORDS:
+        _ORACLE_RECORDS[(N, preset)] = oracle.gen_constellations(N, preset)
+    return _ORACLE_RECORDS[(N, preset)]
+
+
+def take(rec, idx):
+    import oracle
+    return oracle.Records(rec.ld[idx], rec.rd[idx], rec.col[idx], rec.startijkl[idx])
+
+
+def cpu_sample(N: int, frac: float, seed: int):
+    """Seeded subset of the N-workload's records (oracle generator) for the CPU legs."""
+    import numpy as np
+    recs = oracle_records(N, preset_of(N))
     rng = np.random.default_rng(seed)
-    take = max(1, int(round(frac * len(recs))))
-    idx = np.sort(rng.choice(len(recs), size=take, replace=False))
-    sub = recs[idx]
-    return oracle.Records(sub["ld"].astype(np.uint64), sub["rd"].astype(np.uint64), sub["col"].astype(np.uint64),
-                          sub["startijkl"].copy()), len(recs)
+    n = max(1, int(round(frac * len(recs))))
+    idx = np.sort(rng.choice(len(recs), size=n, replace=False))
+    return take(recs, idx), len(recs)
 
 
 def run_cpu(N: int, target_s: float, seed: int = 2026):
     """Oracle port on all host threads over a sample sized to ~target_s seconds; returns nodes/s etc."""
     import oracle
-    oracle.build()
     threads = os.cpu_count() or 1
     # calibrate on a small slice, then size the sample
     rec, m_all = cpu_sample(N, 1 / 512, seed)
@@ -146,31 +173,59 @@ def run_cpu(N: int, target_s: float, seed: int = 2026):
             "frac": frac}
 
 
+def bench_config(N: int):
+    """The workload both arms measure (the same dict on both lines)."""
+    p = preset_of(N)
+    m = len(oracle_records(N, p))
+    return {"workload": f"plain single-N count, N={N}, preset {p} ({m:,} tasks, {expected_total(N):,} solutions)",
+            "N": N, "preset": p, "tasks": m, "l2": "GPU arm: flushed between timed steps (256 MiB write)"}
+
+
 def reference_arm(args):
+    """The reference algorithm's CPU implementation (the oracle port of 356Py's generator and dfs_iter) on all
+    host threads.  The full N=19 task list is cut into `steps` strided slices; timed step i counts slice i, so
+    the timed steps together count every task once and the total must equal the known answer."""
+    import numpy as np
+    import oracle
     ws, rank, _ = dist_env()
     if rank != 0:
         return 0
-    steps = []
-    for _ in range(args.warmup):
-        run_cpu(N_BENCH, 2.0)
-    for _ in range(args.steps):
-        steps.append(run_cpu(N_BENCH, args.cpu_seconds))
-    vals = [s["value"] for s in steps]
-    v = statistics.mean(vals)
-    s0 = steps[0]
-    sample = (f"seeded {s0['frac']:.4f} of the N=19 preset-6 task list ({s0['tasks']} of {s0['tasks_all']} tasks, "
-              f"~{s0['seconds']:.1f} s per step), nodes from the oracle's own dfs_iter counter")
+    threads = os.cpu_count() or 1
+    N = args.n
+    rec = oracle_records(N, preset_of(N))
+    m = len(rec)
+    rng = np.random.default_rng(2026)
+    for _ in range(args.warmup):                       # warm-up: small seeded samples, untimed
+        oracle.exec_solutions(N, take(rec, np.sort(rng.choice(m, size=max(1, m // 512), replace=False))),
+                              threads=threads)
+    K = max(1, args.steps)
+    secs, nodes_total, sol_total = [], 0, 0
+    for i in range(K):
+        sub = take(rec, np.arange(i, m, K))
+        t0 = time.perf_counter()
+        sol, nodes = oracle.exec_solutions(N, sub, threads=threads, want_nodes=True)
+        secs.append(time.perf_counter() - t0)
+        nodes_total += int(nodes.sum())
+        sol_total += int(sol.sum())
+    assert sol_total == expected_total(N), f"reference arm total {sol_total} != {expected_total(N)}"
+    assert nodes_total == DFS_NODES[N]
+    v = nodes_total / sum(secs)
+    sample = (f"the full N={N} preset-{preset_of(N)} task list ({m} tasks, oracle generator) cut into {K} strided "
+              "slices, one per "
+              f"timed step; the steps together count every task once (total {sol_total}); nodes from the oracle's "
+              "own dfs_iter counter")
     line = {
-        "impl": "reference", "metric": METRIC, "value": v, "unit": "nodes/s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(s["seconds"] for s in steps),
+        "impl": "reference", "metric": metric(N), "value": v, "unit": "nodes/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(secs),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-        "config": {"workload": "plain single-N count, N=19, preset 6 (897,071 tasks), CPU sample",
-                   "N": N_BENCH, "preset": 6},
-        "cpu_baseline": {"value": v, "unit": "nodes/s", "cores": s0["cores"], "kind": "port", "sample": sample},
+        "config": bench_config(N),
+        "cpu_baseline": {"value": v, "unit": "nodes/s", "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": v, "unit": "nodes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "note": ("CPU implementation of the reference algorithm (C restatement of 356Py dfs_iter + generator, "
-                 "oracle/nq_oracle.c, pthreads); the reference's own C port (10Bit_CUDA/13CUDA_constellation.c) "
-                 "is built from the reference checkout, which the GPU host does not have"),
+        "total": sol_total, "seconds_total": sum(secs),
+        "note": ("CPU implementation of the reference algorithm (C restatement of 356Py gen_constellations and "
+                 "dfs_iter, oracle/nq_oracle.c, pthreads); the reference's own C port "
+                 "(10Bit_CUDA/13CUDA_constellation.c) is built from the reference checkout, which the GPU host does "
+                 "not have"),
     }
     print(json.dumps(line))
     return 0
@@ -206,8 +261,8 @@ def ours_arm(args):
     dev = local if ws > 1 else 0
     torch.cuda.set_device(dev)
     eng = nqueens.Engine(dev, block=args.block, split=args.split)
-    N = N_BENCH
-    expected = 4968057848
+    N = args.n
+    expected = expected_total(N)
     recs = nqueens.gen_records(N)
     m = len(recs)
     start_min = int((recs["startijkl"] >> 20).min())
@@ -222,7 +277,7 @@ def ours_arm(args):
     for _ in range(args.warmup):
         step()
         eng.sync()
-        assert int(d_total.item()) == expected, "N=19 total mismatch"
+        assert int(d_total.item()) == expected, f"N={N} total mismatch"
     peaks = load_peaks()
     int_peak = eng.int32_peak(0)
     int_peak_add = eng.int32_peak(1)
@@ -274,14 +329,15 @@ def ours_arm(args):
     # the reference's "wall s per N": generation + upload + count + read-back through nq_count
     t0 = time.perf_counter()
     assert eng.count(N).total == expected
-    wall_n19 = time.perf_counter() - t0
+    wall_s = time.perf_counter() - t0
 
     dfs_avg = statistics.mean(dfs_ms)
     achieved_ops = nodes * OPS_PER_NODE / (dfs_avg * 1e-3)
-    traffic = read_traffic()
+    at_profile = N == 19                     # the committed ncu capture is of the N=19 launch
+    traffic = read_traffic() if at_profile else None
     # Executed instructions against the issue limit (one warp instruction per clock per SM sub-partition):
     # the step is issue/math-pipe bound, so this is the fraction that measures the kernel.
-    warp_instr = read_profile_figure("warp_instructions_per_launch")
+    warp_instr = read_profile_figure("warp_instructions_per_launch") if at_profile else None
     sm_count = torch.cuda.get_device_properties(dev).multi_processor_count
     issue = None
     if warp_instr and clk.get("sm_mhz"):
@@ -292,16 +348,14 @@ def ours_arm(args):
                  "source": "instruction count of one ncu capture (profiles/dfs_kernel_n19.md), time of this run, "
                            "peak = SMs x 4 issue slots x median sampled SM clock"}
     line = {
-        "metric": METRIC, "value": value, "unit": "nodes/s", "n_gpus": ws, "steps": args.steps,
+        "metric": metric(N), "value": value, "unit": "nodes/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-        "config": {"workload": "plain single-N count, N=19, preset 6 (897,071 tasks, 4,968,057,848 solutions), "
-                               "one prepare+DFS launch pair per step",
-                   "N": N, "preset": 6, "tasks": m, "block": args.block, "split_depth": split_depth,
-                   "queued_subtasks": queued,
-                   "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{ws}"},
-        "n19_total": expected,
-        "n19_wall_s": wall_n19,
+        "config": bench_config(N),
+        "launch": {"per_step": "one prepare + split + DFS launch sequence", "block": args.block,
+                   "split_depth": split_depth, "queued_subtasks": queued, "parallelism": f"replicas x{ws}"},
+        "total": expected,
+        "wall_s": wall_s,
         "dfs_kernel_ms": dfs_avg,
         "e2e": {"value": ws * nodes / e2e_s, "unit": "nodes/s", "seconds_per_step": e2e_s,
                 "h2d_bytes_per_step": m * 16, "d2h_bytes_per_step": 16},
@@ -310,8 +364,8 @@ def ours_arm(args):
                      "peak_source": "measured in this run: lop3.b32 throughput probe (nq_int32_peak); "
                                     f"add.u32 probe {int_peak_add / 1e9:.0f} Gop/s",
                      "ops_per_node": OPS_PER_NODE, "issue": issue,
-                     "alu_pipe_pct_of_peak_ncu": read_profile_figure("alu_pipe_pct_of_peak"),
-                     "issue_active_pct_ncu": read_profile_figure("issue_active_pct"),
+                     "alu_pipe_pct_of_peak_ncu": read_profile_figure("alu_pipe_pct_of_peak") if at_profile else None,
+                     "issue_active_pct_ncu": read_profile_figure("issue_active_pct") if at_profile else None,
                      "hbm_frac": (m * 16 + m * 16 + m * 8 + m * 4 * 15) / (dfs_avg * 1e-3) / (
                          (peaks or {}).get("hbm_gbs", 6800.0) * 1e9)},
         "clocks": clk,
@@ -320,14 +374,110 @@ def ours_arm(args):
     if rank == 0 and not args.no_cpu:
         cb = run_cpu(N, args.cpu_seconds)
         line["cpu_baseline"] = {"value": cb["value"], "unit": "nodes/s", "cores": cb["cores"], "kind": "port",
-                                "sample": (f"seeded {cb['frac']:.4f} of the N=19 task list ({cb['tasks']} tasks, "
-                                           f"{cb['seconds']:.1f} s), C oracle port, all host threads")}
+                                "sample": (f"seeded {cb['frac']:.4f} of the N={N} task list ({cb['tasks']} tasks, "
+                                           f"oracle generator, {cb['seconds']:.1f} s), C oracle port, all host "
+                                           "threads")}
+    # the metric's second half: the mixed batch and the served stream against one plain launch per job
+    if rank == 0 and not args.no_mix:
+        line["batch"] = batch_figures(eng, max(3, min(args.steps, 5)), value / ws)
+        line["serve"] = serve_figures(eng, args)
     if rank == 0:
         print(json.dumps(line))
     eng.close()
     if ws > 1:
         torch.distributed.destroy_process_group()
     return 0
+
+
+def dfs_ms_alone(eng, N: int, reps: int = 3) -> float:
+    """Device time of N's whole-board DFS launch run alone (records resident, the engine's tuned launch)."""
+    import numpy as np
+    import torch
+    import nqueens
+    recs = nqueens.gen_records(N)
+    start_min = int((recs["startijkl"] >> 20).min())
+    d_rec = torch.from_numpy(recs.view(np.uint8).copy()).cuda()
+    d_total = torch.zeros(1, dtype=torch.int64, device="cuda")
+    eng._apply_tuning(N)
+    ts = []
+    for r in range(reps + 1):
+        eng.exec_device(N, d_rec.data_ptr(), len(recs), start_min, d_total.data_ptr())
+        eng.sync()
+        if r:
+            ts.append(eng.last_kernel_ms()[1])
+    return statistics.median(ts)
+
+
+def batch_figures(eng, reps: int, node_rate: float = 0.0) -> dict:
+    """256 counting jobs, N uniform in 10..18 (numpy default_rng(2026)), tasks resident: one graph-replayed
+    persistent launch against one launch and read-back per job, and the floor both forms share (the sum of each
+    job's DFS kernel time when it runs alone)."""
+    import numpy as np
+    import nqueens
+    import oracle
+    Ns = [int(x) for x in np.random.default_rng(2026).integers(10, 19, size=256)]
+    exp = np.array([oracle.EXPECTED_TOTAL[N] for N in Ns], np.uint64)
+    t0 = time.perf_counter()
+    b = eng.batch([nqueens.CountJob(N) for N in Ns])
+    build_s = time.perf_counter() - t0
+    try:
+        for _ in range(2):
+            assert np.array_equal(b.run(use_graph=True), exp) and np.array_equal(b.run_plain(), exp)
+        tg, tp = [], []
+        for _ in range(reps):
+            t0 = time.perf_counter(); r = b.run(use_graph=True); tg.append(time.perf_counter() - t0)
+            assert np.array_equal(r, exp)
+            t0 = time.perf_counter(); r = b.run_plain(); tp.append(time.perf_counter() - t0)
+            assert np.array_equal(r, exp)
+        tasks, h2d = b.tasks, b.h2d_bytes
+    finally:
+        b.close()
+    alone = {N: dfs_ms_alone(eng, N) for N in sorted(set(Ns))}
+    floor_ms = sum(alone[N] for N in Ns)
+    # the work floor: every job's reference nodes at the full-GPU node rate of the N=19 count (no mix can beat it
+    # by more than the few percent the kernel's pruning varies between boards)
+    work_ms = 1e3 * sum(DFS_NODES[N] for N in Ns) / node_rate if node_rate > 0 else None
+    g, p = statistics.median(tg), statistics.median(tp)
+    return {"workload": "256 counting jobs, N uniform 10..18 (numpy default_rng(2026)), tasks resident",
+            "jobs": len(Ns), "tasks": tasks, "jobs_per_s": len(Ns) / g, "ms": 1e3 * g,
+            "plain_jobs_per_s": len(Ns) / p, "plain_ms": 1e3 * p, "speedup_vs_plain": p / g,
+            "floor_ms": floor_ms, "ms_over_floor": 1e3 * g / floor_ms,
+            "floor": "sum over the 256 jobs of the job's whole-board DFS kernel time alone (CUDA events)",
+            "work_floor_ms": work_ms,
+            "work_floor": "sum over the 256 jobs of the job's reference DFS nodes / this run's N=19 nodes per second",
+            "dfs_ms_alone_by_N": {str(k): round(v, 4) for k, v in alone.items()},
+            "build_s": build_s, "h2d_bytes": h2d, "exact": True, "reps": reps}
+
+
+def serve_figures(eng, args) -> dict:
+    """The served completion stream (N uniform 14..20, k uniform 0..4 pre-placed queens, seeded) offered all at
+    once, so jobs/s is each form's capacity: the continuous-batching server against one plain call per query in
+    arrival order.  Latency = result time - submission time; counts must agree query for query."""
+    import numpy as np
+    from nqueens.server import Server, random_completion_queries, run_plain
+    jobs = random_completion_queries(args.queries, seed=2026, N_range=(14, 20), k_range=(0, 4))
+    run_plain(eng, jobs[:4])                           # warm-up
+    t0 = time.perf_counter()
+    lat_plain, res_plain = [], []
+    for j in jobs:
+        res_plain.append(run_plain(eng, [j])[0])
+        lat_plain.append(time.perf_counter() - t0)
+    span_plain = time.perf_counter() - t0
+    with Server(engine=eng, budget_bytes=args.budget_gb << 30, max_inflight=args.inflight,
+                max_batch_jobs=args.max_batch, large_share=args.large_share) as srv:
+        futs = [srv.submit(j) for j in jobs]
+        srv.drain(600)
+        res_srv = [f.result() for f in futs]
+        st = srv.stats()
+    assert res_srv == res_plain, "served counts differ from the plain per-query counts"
+    pl = np.array(lat_plain)
+    return {"workload": f"{len(jobs)} completion queries (numpy default_rng(2026)), all offered at t=0",
+            "queries": len(jobs), "jobs_per_s": st.jobs_per_s, "p50_ms": 1e3 * st.percentile(50),
+            "p99_ms": 1e3 * st.percentile(99), "batches": st.batches,
+            "plain": {"jobs_per_s": len(jobs) / span_plain, "p50_ms": 1e3 * float(np.percentile(pl, 50)),
+                      "p99_ms": 1e3 * float(np.percentile(pl, 99))},
+            "speedup_vs_plain": st.jobs_per_s * span_plain / len(jobs),
+            "h2d_bytes": st.h2d_bytes, "d2h_bytes": st.d2h_bytes, "exact": True}
 
 
 def batch_arm(args):
@@ -462,6 +612,7 @@ def serve_arm(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--n", type=int, default=N_BENCH, choices=sorted(DFS_NODES), help="board size of the workload")
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
@@ -469,6 +620,7 @@ def main():
     ap.add_argument("--split", type=int, default=-1, help="split depth (-1 automatic)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-mix", action="store_true", help="skip the batch and serve figures of the default line")
     ap.add_argument("--workload", choices=["n19", "batch", "serve"], default="n19",
                     help="n19: the headline single-N count; batch / serve: the batching and serving configs")
     ap.add_argument("--queries", type=int, default=150)

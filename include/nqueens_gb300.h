@@ -49,6 +49,8 @@ void nq_destroy(nq_handle *h);
 int nq_last_error(const nq_handle *h, char *buf, size_t cap);
 /* Name of the handle's GPU (the key of the autotuner's tables). */
 int nq_device_name(const nq_handle *h, char *buf, size_t cap);
+/* Multiprocessor count of the handle's GPU. */
+int nq_device_sms(const nq_handle *h, int *sms);
 
 /* Launch knobs chosen by the autotuner: threads per block (64, 128 or 256),
  * grid (0 = one wave of resident blocks) and split depth (-1 = automatic,
@@ -56,6 +58,14 @@ int nq_device_name(const nq_handle *h, char *buf, size_t cap);
  * the queue holds many small subtasks instead of few large ones). */
 int nq_set_config(nq_handle *h, int block, int grid, int split_depth);
 int nq_get_config(const nq_handle *h, int *block, int *grid, int *split_depth);
+
+/* Order of the DFS queue of single-N counts: 0 = generator order (split
+ * subtasks task after task), 1 = largest estimated subtree first, sorted on
+ * the device.  Replaces the reference's cost-key reorder of its task list
+ * before launch (14Bit_codon_GPU/356Py_savesp_narrow.py:4310-4372, risk table
+ * :3646-3748; sort modes :2445-2541).  Counts do not depend on the order. */
+int nq_set_queue_order(nq_handle *h, int mode);
+int nq_get_queue_order(const nq_handle *h, int *mode);
 
 /* select_dynamic_preset_queens (356Py_savesp_narrow.py:5744-5753). */
 int nq_preset_for(int N);
@@ -108,9 +118,14 @@ int nq_last_run_info(const nq_handle *h, int *split_depth, int64_t *queued);
  * schedules up to 24 depths (N - start_min <= 25); larger inputs are rejected
  * with NQ_EINVAL, never truncated.  No task splitting.  The first call on each
  * device looks the array's address up (cudaGetSymbolAddress) with that device
- * current; make that first call before any stream capture.  Every call shares
- * the one array, so calls that overlap on the GPU race: serialise them.  The
- * call waits for its stream and returns the device status. */
+ * current; with lazy module loading that first call is also when the array
+ * and the kernels are loaded onto the device, so make it once at start-up --
+ * before another allocator reserves the GPU's memory, and before any stream
+ * capture.  The address is kept for the life of the process: after a
+ * cudaDeviceReset of that device the library must be reloaded.  Every call
+ * shares the one array, so calls that overlap on the GPU race: serialise
+ * them.  The call waits for its stream before it returns, and returns the
+ * device status. */
 int nq_exec_solutions_noalloc(int N, const nq_record *d_records, int64_t m, int start_min, uint64_t *d_solutions,
                               uint64_t *d_total, void *stream);
 
@@ -125,8 +140,17 @@ int nq_tune(nq_handle *h, int N, int repeats, int *best_block, int *best_split, 
 /* Whole-board total for N, the loop body of the reference's main()
  * (356Py_savesp_narrow.py:6036-6046): brute force on the GPU for N <= 5
  * (the reference's _bit_total, :5755-5767), the constellation path above.
- * preset <= 0 selects nq_preset_for(N). */
+ * preset <= 0 selects nq_preset_for(N).  The records are generated and
+ * counted in chunks (the reference's streamed generation,
+ * gen_constellations_stream_to_bin, :2988-3084), so host memory stays bounded
+ * at the largest boards: the next chunk is generated while the previous one
+ * counts on the GPU. */
 int nq_count(nq_handle *h, int N, int preset, uint64_t *total);
+/* Records per chunk of nq_count (0: the default, 8 Mi records, about 32 MB of
+ * host records per chunk; one chunk up to N=21). */
+int nq_set_chunk_records(nq_handle *h, int64_t records);
+/* Chunks and records of the handle's last nq_count. */
+int nq_last_count_info(const nq_handle *h, int64_t *chunks, int64_t *records);
 
 /* Unique (distinct under rotation and reflection) and total counts by the
  * symmetry method (11Bit_Python/07Py_bit_symmetry.py:65-200; GPU form
@@ -183,6 +207,13 @@ int nq_resident_blocks(nq_handle *h, int wide, int maxt, int *blocks);
  * size, schedule word and stack depth): the unit nq_batch_set_grid shares out.
  * No counterpart in the reference (it runs one N per process). */
 int nq_batch_resident_blocks(const nq_batch *b, int *blocks);
+/* Upper estimate of the device bytes a batch holding this one job takes
+ * (records, tasks, schedules and split queue) on a GPU with `sms`
+ * multiprocessors at split depth `split_depth` (-1 automatic), computed on the
+ * host without a device or any allocation: admission control sizes a job
+ * before building it.  No counterpart in the reference (it runs one N per
+ * process).  Returns the bytes or a negative status. */
+int64_t nq_job_device_bytes(const nq_job *job, int sms, int split_depth);
 /* Device bytes the batch holds, and host-to-device bytes its build copied
  * (records of count jobs, tasks of completion jobs). */
 int64_t nq_batch_device_bytes(const nq_batch *b);

@@ -21,37 +21,12 @@
 #include "../../include/nqueens_gb300.h"
 #include "nq_common.cuh"
 #include "nq_host.h"
+#include "nq_handle.h"
 #include "nq_internal.h"
 
 using namespace nq;
 
 namespace {
-
-// Device buffer.  With a stream set, allocation and release are stream-ordered
-// (cudaMallocAsync / cudaFreeAsync on that stream), so building or freeing one
-// batch never waits for kernels of other batches still running.
-struct DevBuf {
-  void* p = nullptr;
-  size_t cap = 0;
-  cudaStream_t ordered = nullptr;
-  cudaError_t ensure(size_t n) {
-    if (n <= cap) return cudaSuccess;
-    release();
-    size_t want = std::max<size_t>(n, 256);
-    cudaError_t e = ordered ? cudaMallocAsync(&p, want, ordered) : cudaMalloc(&p, want);
-    if (e == cudaSuccess) cap = want; else p = nullptr;
-    return e;
-  }
-  void release() {
-    if (p) { if (ordered) cudaFreeAsync(p, ordered); else cudaFree(p); }
-    p = nullptr; cap = 0;
-  }
-};
-
-// Control block of one run: totals (u64 per job), queue cursor, error word.
-struct Ctrl {
-  static size_t bytes(int njobs) { return (size_t)njobs * 8 + 16; }
-};
 
 int preset_for(int N) {
   if (N >= 5 && N <= 17) return 5;
@@ -73,6 +48,7 @@ const char* derr_text(uint32_t e) {
   if (e & DERR_SHIFT) return "a record needs a negative shift (preset too deep for N)";
   if (e & DERR_NOTERM) return "a task's schedule never reaches a base frame";
   if (e & DERR_BADN) return "task with N outside 6..27";
+  if (e & DERR_FORMAT) return "a schedule op does not fit the compact schedule word";
   return "ok";
 }
 
@@ -92,6 +68,10 @@ int choose_split(int64_t m, int sms) {
   return (D == 0 && m >= 1000000 && m <= 400000000) ? 1 : D;
 }
 
+// Records per chunk of a whole-board count (nq_count): one chunk up to N=21
+// (2.0 M records), four at N=22 (28.7 M), about 32 MB of host records each.
+constexpr int64_t kChunkRecords = 8 << 20;
+
 int maxt_for(int N, int start_min) {
   // Terminal-parent depth T <= N - 3 - start; one frame of margin.
   int s = start_min < 0 ? 1 : start_min;
@@ -100,76 +80,6 @@ int maxt_for(int N, int start_min) {
 }
 
 }  // namespace
-
-struct nq_handle {
-  int device = 0;
-  int sms = 0;
-  cudaStream_t stream = nullptr;
-  int block = 64, grid = 0, split = -1;    // split: -1 automatic, 0..3 fixed depth
-  std::string err;
-  DevBuf rec, root, info, sched, per_task, ctrl, nsub, sroot, sinfo;
-  uint64_t* h_ctrl = nullptr;   // pinned read-back of the control block
-  size_t h_ctrl_cap = 0;
-  // pinned read-back blocks for batches, reused (freeing pinned memory can
-  // synchronise the device, which would stall other batches in flight)
-  std::mutex pin_mu;
-  std::vector<std::pair<void*, size_t>> pin_free;
-  void* pin_get(size_t bytes) {
-    {
-      std::lock_guard<std::mutex> lk(pin_mu);
-      for (size_t i = 0; i < pin_free.size(); i++)
-        if (pin_free[i].second >= bytes) {
-          void* q = pin_free[i].first;
-          pin_free.erase(pin_free.begin() + (long)i);
-          pinned_sizes[q] = bytes;
-          return q;
-        }
-    }
-    const size_t want = std::max<size_t>(bytes, 65536);
-    void* q = nullptr;
-    if (cudaMallocHost(&q, want) != cudaSuccess) return nullptr;
-    std::lock_guard<std::mutex> lk(pin_mu);
-    pinned_cap[q] = want;
-    pinned_sizes[q] = bytes;
-    return q;
-  }
-  void pin_put(void* q) {
-    if (!q) return;
-    std::lock_guard<std::mutex> lk(pin_mu);
-    pin_free.push_back({q, pinned_cap[q]});
-  }
-  std::map<void*, size_t> pinned_cap, pinned_sizes;
-  bool pending = false;
-  int last_split = 0;        // split depth and queue length of the last run
-  int64_t last_queue = 0;
-  // events around the last run's kernels (same stream as the launches)
-  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
-
-  int fail(int status, const char* fmt, ...) {
-    char buf[512];
-    va_list ap; va_start(ap, fmt); vsnprintf(buf, sizeof buf, fmt, ap); va_end(ap);
-    err = buf;
-    return status;
-  }
-  int cuda_fail(cudaError_t e, const char* where) {
-    return fail(e == cudaErrorMemoryAllocation ? NQ_ENOMEM : NQ_ECUDA, "%s: %s", where, cudaGetErrorString(e));
-  }
-  int ensure_pinned(size_t bytes) {
-    if (bytes <= h_ctrl_cap) return NQ_OK;
-    if (h_ctrl) cudaFreeHost(h_ctrl);
-    h_ctrl = nullptr; h_ctrl_cap = 0;
-    cudaError_t e = cudaMallocHost((void**)&h_ctrl, bytes);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaMallocHost");
-    h_ctrl_cap = bytes;
-    return NQ_OK;
-  }
-};
-
-#define NQ_CUDA(h, call)                                     \
-  do {                                                       \
-    cudaError_t _e = (call);                                 \
-    if (_e != cudaSuccess) return (h)->cuda_fail(_e, #call); \
-  } while (0)
 
 namespace {
 
@@ -186,22 +96,22 @@ int run_records(nq_handle* h, int N, const uint4* d_rec, int64_t m, int start_mi
   NQ_CUDA(h, h->root.ensure((size_t)m * sizeof(uint4)));
   NQ_CUDA(h, h->info.ensure((size_t)m * sizeof(uint2)));
   NQ_CUDA(h, h->sched.ensure((size_t)m * sw * sizeof(uint32_t)));
-  NQ_CUDA(h, h->ctrl.ensure(Ctrl::bytes(1) + 16));
+  NQ_CUDA(h, h->ctrl.ensure(ctl::kBytes));
   unsigned char* c = (unsigned char*)h->ctrl.p;
-  NQ_CUDA(h, cudaMemsetAsync(c, 0, Ctrl::bytes(1) + 16, st));
+  NQ_CUDA(h, cudaMemsetAsync(c, 0, ctl::kBytes, st));
   TaskArrays ta;
   ta.root = (uint4*)h->root.p; ta.info = (uint2*)h->info.p; ta.sched = h->sched.p; ta.sw = sw; ta.wide = false;
-  unsigned long long* totals = (unsigned long long*)c;
-  unsigned int* cursor = (unsigned int*)(c + 8);
-  unsigned int* err = (unsigned int*)(c + 12);
-  unsigned long long* sctr = (unsigned long long*)(c + 16);   // split: [0] subtasks, [1] allocation cursor
-  unsigned int* tmax = (unsigned int*)(c + 32);                // deepest schedule of the launch
+  unsigned long long* totals = (unsigned long long*)(c + ctl::kTotal);
+  unsigned long long* cursor = (unsigned long long*)(c + ctl::kCursor);
+  unsigned int* err = (unsigned int*)(c + ctl::kErr);
+  unsigned long long* sctr = (unsigned long long*)(c + ctl::kSplit);   // split: [0] subtasks, [1] allocation cursor
+  unsigned int* tmax = (unsigned int*)(c + ctl::kTmax);                 // deepest schedule of the launch
   NQ_CUDA(h, cudaEventRecord(h->ev[0], st));
   NQ_CUDA(h, launch_prepare(N, m, d_rec, ta, 0, 0, err, st, tmax));
   const int D = h->split >= 0 ? h->split : choose_split(m, h->sms);
   DfsLaunch L;
   L.tasks = ta; L.m = m; L.order = nullptr; L.cursor = cursor; L.job_totals = totals;
-  L.per_task = d_per_task; L.err = err; L.maxt = maxt; L.block = h->block; L.grid = h->grid; L.big = N >= 24;
+  L.per_task = d_per_task; L.err = err; L.maxt = maxt; L.block = h->block; L.grid = h->grid;
   if (D > 0) {
     NQ_CUDA(h, h->nsub.ensure((size_t)m * sizeof(uint32_t)));
     NQ_CUDA(h, launch_split(0, D, 0, m, ta, (uint32_t*)h->nsub.p, nullptr, nullptr, sctr, nullptr, totals, 0, st));
@@ -209,19 +119,29 @@ int run_records(nq_handle* h, int N, const uint4* d_rec, int64_t m, int start_mi
   // One read-back: the split size and the deepest schedule T.  Subtasks start
   // at depth D with an empty stack, so the DFS needs T - D frames and T - D + 1
   // schedule words per lane; the kernel still rejects any task deeper than that.
-  if (int s = h->ensure_pinned(Ctrl::bytes(1) + 16)) return s;
-  NQ_CUDA(h, cudaMemcpyAsync(h->h_ctrl, c, Ctrl::bytes(1) + 16, cudaMemcpyDeviceToHost, st));
+  if (int s = h->ensure_pinned(ctl::kBytes)) return s;
+  NQ_CUDA(h, cudaMemcpyAsync(h->h_ctrl, c, ctl::kBytes, cudaMemcpyDeviceToHost, st));
   NQ_CUDA(h, cudaStreamSynchronize(st));
-  const int t_deep = (int)(uint32_t)h->h_ctrl[4];
+  const unsigned char* hc = (const unsigned char*)h->h_ctrl;
+  const int t_deep = (int)*(const uint32_t*)(hc + ctl::kTmax);
   L.maxt = std::max(1, std::min(maxt, t_deep - D));
   if (D > 0) {
-    const int64_t ns = (int64_t)h->h_ctrl[2];
+    const int64_t ns = (int64_t)*(const uint64_t*)(hc + ctl::kSplit);
     if (ns > (int64_t)0xFFFFFFFF) return h->fail(NQ_ENOMEM, "split: %lld subtasks", (long long)ns);
     NQ_CUDA(h, h->sroot.ensure((size_t)std::max<int64_t>(ns, 1) * sizeof(uint4)));
     NQ_CUDA(h, h->sinfo.ensure((size_t)std::max<int64_t>(ns, 1) * sizeof(uint2)));
     NQ_CUDA(h, launch_split(1, D, 0, m, ta, (uint32_t*)h->nsub.p, (uint4*)h->sroot.p, (uint2*)h->sinfo.p, sctr,
                             d_per_task, totals, 0, st));
     L.sroot = (const uint4*)h->sroot.p; L.sinfo = (const uint2*)h->sinfo.p; L.m = ns;
+  }
+  L.big = counts_need_u64(N, L.m);
+  if (h->queue_order == 1) {
+    NQ_CUDA(h, h->okeys.ensure((size_t)std::max<int64_t>(L.m, 1)));
+    NQ_CUDA(h, h->oorder.ensure((size_t)std::max<int64_t>(L.m, 1) * sizeof(uint32_t)));
+    NQ_CUDA(h, h->ohist.ensure(512 * sizeof(unsigned int)));
+    NQ_CUDA(h, launch_order(L.m, L.sroot, L.sinfo, ta, (uint8_t*)h->okeys.p, (unsigned int*)h->ohist.p,
+                            (uint32_t*)h->oorder.p, st));
+    L.order = (const uint32_t*)h->oorder.p;
   }
   h->last_split = D; h->last_queue = L.m;
   NQ_CUDA(h, cudaEventRecord(h->ev[1], st));
@@ -231,12 +151,13 @@ int run_records(nq_handle* h, int N, const uint4* d_rec, int64_t m, int start_mi
 }
 
 int read_ctrl(nq_handle* h, cudaStream_t st, uint64_t* total) {
-  if (int s = h->ensure_pinned(Ctrl::bytes(1))) return s;
-  NQ_CUDA(h, cudaMemcpyAsync(h->h_ctrl, h->ctrl.p, Ctrl::bytes(1), cudaMemcpyDeviceToHost, st));
+  if (int s = h->ensure_pinned(ctl::kBytes)) return s;
+  NQ_CUDA(h, cudaMemcpyAsync(h->h_ctrl, h->ctrl.p, ctl::kBytes, cudaMemcpyDeviceToHost, st));
   NQ_CUDA(h, cudaStreamSynchronize(st));
-  const uint32_t e = ((const uint32_t*)h->h_ctrl)[3];
+  const unsigned char* hc = (const unsigned char*)h->h_ctrl;
+  const uint32_t e = *(const uint32_t*)(hc + ctl::kErr);
   if (e) return h->fail(derr_to_status(e), "device: %s", derr_text(e));
-  if (total) *total = h->h_ctrl[0];
+  if (total) *total = *(const uint64_t*)(hc + ctl::kTotal);
   return NQ_OK;
 }
 
@@ -272,7 +193,8 @@ int nq_create(nq_handle** out, int device) {
   if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
       cudaEventCreate(&h->ev[0]) != cudaSuccess || cudaEventCreate(&h->ev[1]) != cudaSuccess ||
-      cudaEventCreate(&h->ev[2]) != cudaSuccess) {
+      cudaEventCreate(&h->ev[2]) != cudaSuccess ||
+      cudaEventCreateWithFlags(&h->done, cudaEventDisableTiming) != cudaSuccess) {
     nq_destroy(h);
     return NQ_ECUDA;
   }
@@ -286,9 +208,12 @@ void nq_destroy(nq_handle* h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   h->rec.release(); h->root.release(); h->info.release(); h->sched.release(); h->per_task.release(); h->ctrl.release();
   h->nsub.release(); h->sroot.release(); h->sinfo.release();
+  h->okeys.release(); h->oorder.release(); h->ohist.release();
+  h->utasks.release(); h->uconfs.release(); h->uctl.release();
   if (h->h_ctrl) cudaFreeHost(h->h_ctrl);
   for (auto& q : h->pinned_cap) cudaFreeHost(q.first);
   for (auto& e : h->ev) if (e) cudaEventDestroy(e);
+  if (h->done) cudaEventDestroy(h->done);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
 }
@@ -337,6 +262,12 @@ int nq_last_kernel_ms(nq_handle* h, float* prepare_ms, float* dfs_ms) {
   return NQ_OK;
 }
 
+int nq_device_sms(const nq_handle* h, int* sms) {
+  if (!h || !sms) return NQ_EINVAL;
+  *sms = h->sms;
+  return NQ_OK;
+}
+
 int nq_device_name(const nq_handle* h, char* buf, size_t cap) {
   if (!h || !buf || cap == 0) return NQ_EINVAL;
   cudaDeviceProp p;
@@ -356,6 +287,19 @@ int nq_set_config(nq_handle* h, int block, int grid, int split_depth) {
   if (block != 64 && block != 128 && block != 256) return h->fail(NQ_EINVAL, "block must be 64, 128 or 256");
   if (grid < 0 || split_depth < -1 || split_depth > 3) return h->fail(NQ_EINVAL, "bad grid or split depth");
   h->block = block; h->grid = grid; h->split = split_depth;
+  return NQ_OK;
+}
+
+int nq_set_queue_order(nq_handle* h, int mode) {
+  if (!h) return NQ_EINVAL;
+  if (mode != 0 && mode != 1) return h->fail(NQ_EINVAL, "queue order must be 0 or 1");
+  h->queue_order = mode;
+  return NQ_OK;
+}
+
+int nq_get_queue_order(const nq_handle* h, int* mode) {
+  if (!h || !mode) return NQ_EINVAL;
+  *mode = h->queue_order;
   return NQ_OK;
 }
 
@@ -427,6 +371,7 @@ int nq_exec_solutions_device(nq_handle* h, int N, const nq_record* d_records, in
   }
   if (int s = run_records(h, N, (const uint4*)d_records, m, start_min, (unsigned long long*)d_solutions, st)) return s;
   NQ_CUDA(h, cudaMemcpyAsync(d_total, h->ctrl.p, 8, cudaMemcpyDeviceToDevice, st));
+  NQ_CUDA(h, cudaEventRecord(h->done, st));
   h->pending = true;
   return NQ_OK;
 }
@@ -434,11 +379,16 @@ int nq_exec_solutions_device(nq_handle* h, int N, const nq_record* d_records, in
 int nq_sync(nq_handle* h) {
   if (!h) return NQ_EINVAL;
   NQ_CUDA(h, cudaSetDevice(h->device));
-  NQ_CUDA(h, cudaDeviceSynchronize());
-  if (!h->pending) return NQ_OK;
+  if (!h->pending) {                      // nothing asynchronous outstanding: the handle's own stream
+    NQ_CUDA(h, cudaStreamSynchronize(h->stream));
+    return NQ_OK;
+  }
+  // waits for this handle's last count only (its event), not for other handles, batches or streams
+  NQ_CUDA(h, cudaEventSynchronize(h->done));
   h->pending = false;
   uint32_t e = 0;
-  NQ_CUDA(h, cudaMemcpy(&e, (unsigned char*)h->ctrl.p + 12, 4, cudaMemcpyDeviceToHost));
+  NQ_CUDA(h, cudaMemcpyAsync(&e, (unsigned char*)h->ctrl.p + ctl::kErr, 4, cudaMemcpyDeviceToHost, h->stream));
+  NQ_CUDA(h, cudaStreamSynchronize(h->stream));
   if (e) return h->fail(derr_to_status(e), "device: %s", derr_text(e));
   return NQ_OK;
 }
@@ -455,7 +405,10 @@ int nq_debug_task_schedule(int N, nq_record rec, uint32_t root[4], uint32_t* inf
   root[0] = rt.ld; root[1] = rt.rd; root[2] = rt.col; root[3] = (T < 0) ? 0u : rt.avail;
   *info = info_pack(T < 0 ? INFO_NO_DFS : (uint32_t)T, (uint32_t)t.wexp, rc, (uint32_t)N, TS_OK);
   if (T < 0) return 0;
-  for (int d = 0; d <= T; d++) words[d] = pack_compact(ops[d]);
+  for (int d = 0; d <= T; d++) {
+    if (!compact_fits(ops[d], N)) return NQ_EINVAL;
+    words[d] = pack_compact(ops[d]);
+  }
   return T + 1;
 }
 
@@ -531,18 +484,79 @@ int nq_tune(nq_handle* h, int N, int repeats, int* best_block, int* best_split, 
   return NQ_OK;
 }
 
+int nq_set_chunk_records(nq_handle* h, int64_t records) {
+  if (!h) return NQ_EINVAL;
+  if (records < 0) return h->fail(NQ_EINVAL, "chunk size must be >= 0");
+  h->chunk_records = records;
+  return NQ_OK;
+}
+
+// Whole-board count, generated and counted chunk by chunk so host memory stays
+// bounded for the largest boards (the reference streams its task list to a
+// .bin file for the same reason, gen_constellations_stream_to_bin,
+// 356Py_savesp_narrow.py:2988-3084): the start constellations are listed
+// first (cheap), then each chunk of them is expanded into records on the host
+// threads while the previous chunk's DFS runs on the GPU.
 int nq_count(nq_handle* h, int N, int preset, uint64_t* total) {
   if (!h || !total) return NQ_EINVAL;
   if (N < 1 || N > kMaxN) return h->fail(NQ_EINVAL, "N=%d outside 1..27", N);
   if (N <= 5) return nq_count_completions(h, N, 0, nullptr, nullptr, total);
   const int p = preset > 0 ? preset : preset_for(N);
-  std::vector<GenRecord> v;
-  const int s = gen_constellations(N, p, v, 0);
-  if (s == -1) return h->fail(NQ_EINVAL, "generator: bad arguments N=%d preset=%d", N, p);
-  if (s == -2) return h->fail(NQ_EPRESET, "generator: preset %d too deep for N=%d", p, N);
-  std::vector<nq_record> r(v.size());
-  for (size_t i = 0; i < v.size(); i++) r[i] = nq_record{(uint32_t)v[i].ld, (uint32_t)v[i].rd, (uint32_t)v[i].col, v[i].startijkl};
-  return nq_exec_solutions(h, N, r.data(), (int64_t)r.size(), nullptr, total);
+  if (p < 4) return h->fail(NQ_EPRESET, "generator: preset %d below 4", p);
+  std::vector<int> starts;
+  if (start_constellations(N, starts) != 0) return h->fail(NQ_EINVAL, "generator: bad arguments N=%d", N);
+  const int64_t chunk = h->chunk_records > 0 ? h->chunk_records : kChunkRecords;
+  size_t next = 0;
+  double per_start = 0.0;                  // records per start constellation seen so far
+  std::vector<GenRecord> g;
+  auto gen_chunk = [&](std::vector<nq_record>& out) -> int {
+    out.clear();
+    g.clear();
+    while (next < starts.size() && (int64_t)g.size() < chunk) {
+      const double want = (double)(chunk - (int64_t)g.size());
+      const size_t take = per_start > 0.0 ? (size_t)std::max(1.0, want / per_start) : (size_t)16;
+      const size_t s1 = std::min(starts.size(), next + take);
+      const size_t before = g.size();
+      const int e = expand_starts(N, p, starts, next, s1, g, 0);
+      if (e == -1) return h->fail(NQ_EINVAL, "generator: bad arguments N=%d preset=%d", N, p);
+      if (e == -2) return h->fail(NQ_EPRESET, "generator: preset %d too deep for N=%d", p, N);
+      per_start = 0.5 * per_start + 0.5 * (double)(g.size() - before) / (double)(s1 - next);
+      if (per_start <= 0.0) per_start = 0.25;
+      next = s1;
+    }
+    out.resize(g.size());
+    for (size_t i = 0; i < g.size(); i++) out[i] = nq_record{(uint32_t)g[i].ld, (uint32_t)g[i].rd, (uint32_t)g[i].col, g[i].startijkl};
+    return NQ_OK;
+  };
+  cudaStream_t st = h->stream;
+  NQ_CUDA(h, cudaSetDevice(h->device));
+  std::vector<nq_record> cur, nxt;
+  if (int e = gen_chunk(cur)) return e;
+  uint64_t acc = 0;
+  int64_t chunks = 0, records = 0;
+  while (!cur.empty()) {
+    const int64_t m = (int64_t)cur.size();
+    const int smin = (int)start_row_min(&cur[0].startijkl, m, 4);
+    NQ_CUDA(h, h->rec.ensure((size_t)m * sizeof(nq_record)));
+    NQ_CUDA(h, cudaMemcpyAsync(h->rec.p, cur.data(), (size_t)m * sizeof(nq_record), cudaMemcpyHostToDevice, st));
+    if (int s = run_records(h, N, (const uint4*)h->rec.p, m, smin, nullptr, st)) return s;
+    if (int e = gen_chunk(nxt)) { cudaStreamSynchronize(st); return e; }   // overlaps the DFS just launched
+    uint64_t t = 0;
+    if (int s = read_ctrl(h, st, &t)) return s;
+    acc += t; chunks++; records += m;
+    cur.swap(nxt);
+  }
+  h->last_chunks = chunks;
+  h->last_records = records;
+  *total = acc;
+  return NQ_OK;
+}
+
+int nq_last_count_info(const nq_handle* h, int64_t* chunks, int64_t* records) {
+  if (!h) return NQ_EINVAL;
+  if (chunks) *chunks = h->last_chunks;
+  if (records) *records = h->last_records;
+  return NQ_OK;
 }
 
 }  // extern "C"
@@ -559,7 +573,7 @@ struct nq_batch {
   int64_t m = 0;        // tasks
   int64_t ms = 0;       // queued subtasks (every job's split output, job after job)
   int maxt = 1, sw = 2, grid = 0, block = 128;
-  bool big = false;                        // some job has N >= 24: u64 per-task counters
+  bool big = false;                        // some job's queue items may count 2^32: u64 per-lane counters
   bool wide = true;                        // 8-byte schedule words (completion tasks); compact otherwise
   std::vector<int64_t> job_off, job_m;     // task range per job
   std::vector<int64_t> sub_off, sub_m;     // subtask range per job
@@ -590,8 +604,8 @@ int batch_enqueue(nq_batch* b, int use_graph) {
     ta.root = (uint4*)b->root.p; ta.info = (uint2*)b->info.p; ta.sched = b->sched.p; ta.sw = b->sw; ta.wide = b->wide;
     DfsLaunch L;
     L.tasks = ta; L.sroot = (const uint4*)b->sroot.p; L.sinfo = (const uint2*)b->sinfo.p;
-    L.m = b->ms; L.cursor = (unsigned int*)(c + (size_t)nj * 8);
-    L.job_totals = (unsigned long long*)c; L.err = (unsigned int*)(c + (size_t)nj * 8 + 4);
+    L.m = b->ms; L.cursor = (unsigned long long*)(c + (size_t)nj * 8);
+    L.job_totals = (unsigned long long*)c; L.err = (unsigned int*)(c + (size_t)nj * 8 + 8);
     L.maxt = b->maxt; L.block = b->block; L.grid = b->grid; L.big = b->big;
     e = launch_dfs(L, st);
     if (e != cudaSuccess) return e;
@@ -622,7 +636,7 @@ int batch_enqueue(nq_batch* b, int use_graph) {
 int batch_collect(nq_batch* b, uint64_t* totals) {
   nq_handle* h = b->h;
   const int nj = (int)b->jobs.size();
-  const uint32_t e = ((const uint32_t*)(b->h_out + nj))[1];
+  const uint32_t e = ((const uint32_t*)(b->h_out + nj))[2];
   b->submitted = false;
   if (e) return h->fail(derr_to_status(e), "device: %s", derr_text(e));
   if (totals)
@@ -710,7 +724,6 @@ int nq_batch_create(nq_handle* h, const nq_job* jobs, int njobs, nq_batch** out)
   if (maxt >= kMaxDepth) { nq_batch_destroy(b); return h->fail(NQ_ESTACK, "batch: schedule too deep"); }
   b->maxt = maxt; b->sw = maxt + 1;
   b->wide = !htasks.empty();             // constellation-only batches keep the compact 4-byte words
-  for (int j = 0; j < njobs; j++) b->big = b->big || jobs[j].N >= 24;
   const int64_t m_rec = (int64_t)recs.size(), m_host = (int64_t)htasks.size();
   b->m = m_rec + m_host;
   for (auto& sg : segs) { b->job_off[sg.job] = sg.rec_off; b->job_m[sg.job] = sg.m; }
@@ -736,7 +749,7 @@ int nq_batch_create(nq_handle* h, const nq_job* jobs, int njobs, nq_batch** out)
   TaskArrays ta;
   ta.root = (uint4*)b->root.p; ta.info = (uint2*)b->info.p; ta.sched = b->sched.p; ta.sw = b->sw; ta.wide = b->wide;
   unsigned char* c = (unsigned char*)b->ctrl.p;
-  unsigned int* derr = (unsigned int*)(c + (size_t)njobs * 8 + 4);
+  unsigned int* derr = (unsigned int*)(c + (size_t)njobs * 8 + 8);
   cudaStream_t st = b->stream;
   int status = NQ_OK;
   DevBuf jt;                                   // deepest schedule per job (constellation jobs)
@@ -773,7 +786,7 @@ int nq_batch_create(nq_handle* h, const nq_job* jobs, int njobs, nq_batch** out)
     }
     if ((e = cudaMemcpyAsync(b->h_out, c, cb, cudaMemcpyDeviceToHost, st)) != cudaSuccess) break;
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) break;
-    const uint32_t de = ((const uint32_t*)(b->h_out + njobs))[1];
+    const uint32_t de = ((const uint32_t*)(b->h_out + njobs))[2];
     if (de) { status = h->fail(derr_to_status(de), "batch prepare: %s", derr_text(de)); break; }
     // Split each job on its own (tiny boards are not split), so every job's
     // subtasks form one contiguous queue range: pass 0 counts per job, then
@@ -797,6 +810,7 @@ int nq_batch_create(nq_handle* h, const nq_job* jobs, int njobs, nq_batch** out)
     if (e != cudaSuccess) { sctr.release(); break; }
     int64_t total_sub = 0;
     for (int j = 0; j < njobs; j++) { b->sub_off[j] = total_sub; b->sub_m[j] = (int64_t)cnts[2 * j]; total_sub += b->sub_m[j]; }
+    for (int j = 0; j < njobs; j++) b->big = b->big || (b->sub_m[j] > 0 && counts_need_u64(jobs[j].N, b->sub_m[j]));
     b->ms = total_sub;
     // Stacks sized to the deepest subtask: a job's subtasks start at depth
     // job_split[j], so they need (deepest T) - job_split[j] frames.
@@ -825,6 +839,45 @@ int nq_batch_create(nq_handle* h, const nq_job* jobs, int njobs, nq_batch** out)
   if (status != NQ_OK) { nq_batch_destroy(b); return status; }
   *out = b;
   return NQ_OK;
+}
+
+int64_t nq_job_device_bytes(const nq_job* job, int sms, int split_depth) {
+  if (!job || sms < 1 || split_depth < -1 || split_depth > 3) return NQ_EINVAL;
+  const nq_job& J = *job;
+  if (J.N < 1 || J.N > kMaxN || J.k < 0 || J.k > 8) return NQ_EINVAL;
+  int64_t m = 0;
+  size_t word = 0;
+  int maxt = 1;
+  if (J.kind == NQ_JOB_COUNT && J.N >= 6) {
+    // the generator's record count, as nq_batch_create builds the job (compact schedule words)
+    const int p = J.preset > 0 ? J.preset : preset_for(J.N);
+    std::vector<GenRecord> v;
+    const int s = gen_constellations(J.N, p, v, 0);
+    if (s != 0) return s == -2 ? NQ_EPRESET : NQ_EINVAL;
+    m = (int64_t)v.size();
+    int smin = 64;
+    for (const GenRecord& r : v) smin = std::min<int>(smin, (int)(r.startijkl >> 20));
+    maxt = maxt_for(J.N, smin);
+    word = sizeof(uint32_t);
+  } else if (J.kind == NQ_JOB_COUNT || J.kind == NQ_JOB_COMPLETION) {
+    int rows[8], cols[8];
+    const int k = (J.kind == NQ_JOB_COUNT) ? 0 : J.k;
+    for (int q = 0; q < k; q++) { rows[q] = J.rows[q]; cols[q] = J.cols[q]; }
+    std::vector<HostTask> t;
+    int mt = 0;
+    if (build_completion_tasks(J.N, k, rows, cols, 4096, 0, t, &mt) < 0) return NQ_EINVAL;
+    m = (int64_t)t.size();
+    maxt = std::max(1, mt);
+    word = sizeof(uint2);
+  } else {
+    return NQ_EINVAL;
+  }
+  // split queue: each level multiplies the items by at most ~8 (measured 6.2-8x)
+  const int D = (J.N <= 12) ? 0 : (split_depth >= 0 ? split_depth : choose_split(m, sms));
+  int64_t ns = m;
+  for (int d = 0; d < D; d++) ns *= 8;
+  const int64_t per_task = 16 /*record*/ + 16 /*root*/ + 8 /*info*/ + 4 /*split count*/ + (int64_t)(maxt + 1) * (int64_t)word;
+  return m * per_task + ns * (16 + 8) + (int64_t)Ctrl::bytes(1) + 4096;
 }
 
 int nq_batch_set_grid(nq_batch* b, int grid) {
@@ -888,19 +941,19 @@ int nq_batch_run_plain(nq_batch* b, uint64_t* totals) {
   for (int j = 0; j < nj; j++) {
     uint64_t t = 0;
     if (b->sub_m[j] > 0) {
-      NQ_CUDA(h, cudaMemsetAsync(c, 0, 16, b->stream));
+      NQ_CUDA(h, cudaMemsetAsync(c, 0, 24, b->stream));
       TaskArrays ta;
       ta.root = (uint4*)b->root.p; ta.info = (uint2*)b->info.p; ta.sched = b->sched.p; ta.sw = b->sw; ta.wide = b->wide;
       // One job per launch over its subtask range; its tasks carry job id j, which lands in slot 0.
       DfsLaunch L;
       L.tasks = ta; L.sroot = (const uint4*)b->sroot.p + b->sub_off[j]; L.sinfo = (const uint2*)b->sinfo.p + b->sub_off[j];
-      L.m = b->sub_m[j]; L.cursor = (unsigned int*)(c + 8);
-      L.job_totals = (unsigned long long*)c; L.job_base = (uint32_t)j; L.err = (unsigned int*)(c + 12);
-      L.maxt = b->job_maxt[j]; L.block = b->block; L.grid = b->grid; L.big = b->jobs[j].N >= 24;
+      L.m = b->sub_m[j]; L.cursor = (unsigned long long*)(c + 8);
+      L.job_totals = (unsigned long long*)c; L.job_base = (uint32_t)j; L.err = (unsigned int*)(c + 16);
+      L.maxt = b->job_maxt[j]; L.block = b->block; L.grid = b->grid; L.big = counts_need_u64(b->jobs[j].N, b->sub_m[j]);
       NQ_CUDA(h, launch_dfs(L, b->stream));
-      NQ_CUDA(h, cudaMemcpyAsync(b->h_out, c, 16, cudaMemcpyDeviceToHost, b->stream));
+      NQ_CUDA(h, cudaMemcpyAsync(b->h_out, c, 24, cudaMemcpyDeviceToHost, b->stream));
       NQ_CUDA(h, cudaStreamSynchronize(b->stream));
-      const uint32_t e = ((const uint32_t*)b->h_out)[3];
+      const uint32_t e = ((const uint32_t*)b->h_out)[4];
       if (e) return h->fail(derr_to_status(e), "device: %s", derr_text(e));
       t = b->h_out[0];
     }

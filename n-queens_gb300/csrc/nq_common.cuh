@@ -23,8 +23,18 @@
 //         than column 0 is free, the word's LA carries bit 0);
 //         TALL: count every candidate (completion queries, last free row)
 //
-// Compact word (4 B, single-N plain path):
-//   bits 0-1 LA | bits 2-24 RA | 25 FC | 26 TERM | 28 TALL | 29-31 s
+// Compact word (4 B, constellation tasks), laid out so the DFS forms the
+// child masks with two funnel shifts and no field extraction:
+//   bits 0-4     s (1..3): the count of both shifts (a funnel shift reads
+//                only the low 5 bits of its count)
+//   RA << s      at its own position, bits N-1..N: or-ed into rd | bit before
+//                the right shift, ((rd | bit) | RA << s) >> s = nrd
+//   bit 28       FC
+//   top s bits   LA: shf.l(lo = w, hi = x, n = w) = (x << s) | (w >> (32 - s))
+//                = (x << s) | LA
+// TERM is not stored: it is the task's terminal depth T (info word); TALL
+// never occurs in constellation tasks.  compact_fits() checks the fields do
+// not overlap (la < 2^s, RA << s within bits N-1..N).
 // Wide word (8 B, mixed batches and completion queries):
 //   x: bits 0-23 LA | 24-26 s | 27 FC | 28 TERM | 30 TALL;  y: RA
 #pragma once
@@ -42,18 +52,35 @@ constexpr int kMaxN = 27;        // columns in bits 0-26, a frame's depth in bit
 constexpr int kMaxDepth = 28;    // schedule words per task (depths 0..T)
 
 // compact word fields
-constexpr uint32_t C_LA = 0x3u;
-constexpr uint32_t C_RA = 0x01FFFFFCu;
-constexpr uint32_t C_FC = 1u << 25;
-constexpr uint32_t C_TERM = 1u << 26;
-constexpr uint32_t C_TALL = 1u << 28;
-constexpr int C_SSHIFT = 29;   // s in 1..3: walk_schedule steps 1, 2 or 3 rows (the DFS forms 1 << s as s*s - s + 2)
+constexpr uint32_t C_S = 0x1Fu;
+constexpr uint32_t C_FC = 1u << 28;
+NQ_HD uint32_t compact_ra_mask(int N) { return 3u << (N - 1); }   // where RA << s may sit
 // wide word fields (x)
 constexpr uint32_t W_LA = 0x00FFFFFFu;
 constexpr int W_SSHIFT = 24;
 constexpr uint32_t W_FC = 1u << 27;
 constexpr uint32_t W_TERM = 1u << 28;
 constexpr uint32_t W_TALL = 1u << 30;
+
+// Known whole-board totals (the reference's known-answer table,
+// 356Py_savesp_narrow.py:5775), index N.  Used only as an upper bound when
+// sizing counters, never as a result.
+NQ_HD uint64_t known_total(int N) {
+  constexpr uint64_t t[28] = {1ull, 1ull, 0ull, 0ull, 2ull, 10ull, 4ull, 40ull, 92ull, 352ull, 724ull, 2680ull, 14200ull,
+                              73712ull, 365596ull, 2279184ull, 14772512ull, 95815104ull, 666090624ull, 4968057848ull,
+                              39029188884ull, 314666222712ull, 2691008701644ull, 24233937684440ull,
+                              227514171973736ull, 2207893435808352ull, 22317699616364044ull, 234907967154122528ull};
+  return (N >= 0 && N <= 27) ? t[N] : ~0ull;
+}
+
+// Per-lane counts of the DFS are u32 unless a queue item could count 2^32
+// solutions.  An item's share of the board total, measured with the oracle at
+// N=14..17 and presets 4-5, is at most ~2.2x the average (total / 2 / items);
+// a factor of 32 on the average leaves ~15x margin.
+inline bool counts_need_u64(int N, int64_t items) {
+  const double avg = (double)known_total(N) / (double)(items > 0 ? items : 1);
+  return avg * 32.0 >= 4294967296.0;
+}
 
 // Task info word: T (terminal depth, 0..31) | wexp<<5 | root_count<<7 | N<<8 |
 // status<<13.  T == 31 marks a task with no DFS work (root handled in prepare).
@@ -67,7 +94,7 @@ NQ_HD uint32_t info_root(uint32_t x) { return (x >> 7) & 1u; }
 NQ_HD uint32_t info_N(uint32_t x) { return (x >> 8) & 31u; }
 NQ_HD uint32_t info_status(uint32_t x) { return (x >> 13) & 7u; }
 // task status codes stored in the info word
-constexpr uint32_t TS_OK = 0, TS_BAD_SHIFT = 1, TS_DEPTH = 2, TS_NOTERM = 3, TS_BADN = 4;
+constexpr uint32_t TS_OK = 0, TS_BAD_SHIFT = 1, TS_DEPTH = 2, TS_NOTERM = 3, TS_BADN = 4, TS_FORMAT = 5;
 
 // ---------------------------------------------------------------------------
 // SQ* state machine tables (356Py:2236-2289, 2586-2589).
@@ -262,9 +289,25 @@ NQ_HD int walk_schedule(int N, const TaskHead& t, Root* root, uint32_t* root_cou
   }
 }
 
+// True when the op packs into a compact word without overlapping fields.
+NQ_HD bool compact_fits(const Op& o, int N) {
+  if (o.s < 1 || o.s > 3 || o.tall || o.la >= (1u << o.s)) return false;
+  const uint64_t ra = (uint64_t)o.ra << o.s;
+  return (ra & ~(uint64_t)compact_ra_mask(N)) == 0;
+}
 NQ_HD uint32_t pack_compact(const Op& o) {
-  return (o.la & C_LA) | (o.ra & C_RA) | (o.fc ? C_FC : 0u) | (o.term ? C_TERM : 0u) |
-         (o.tall ? C_TALL : 0u) | (o.s << C_SSHIFT);
+  return o.s | (o.ra << o.s) | (o.fc ? C_FC : 0u) | (o.s ? (o.la << (32 - o.s)) : 0u);
+}
+// The op of a compact word (split kernel and host checks); `term`: the word's depth is T.
+NQ_HD Op unpack_compact(uint32_t w, int N, bool term) {
+  Op o;
+  o.s = w & C_S;
+  o.la = w >> (32 - o.s);
+  o.ra = (w & compact_ra_mask(N)) >> o.s;
+  o.fc = (w & C_FC) ? 1u : 0u;
+  o.term = term ? 1u : 0u;
+  o.tall = 0;
+  return o;
 }
 NQ_HD uint32_t pack_wide_x(const Op& o) {
   return (o.la & W_LA) | (o.s << W_SSHIFT) | (o.fc ? W_FC : 0u) | (o.term ? W_TERM : 0u) |

@@ -130,9 +130,9 @@ bool rotated_present(const std::vector<uint8_t>& S, int i, int j, int k, int l, 
 
 }  // namespace
 
-int gen_constellations(int N, int preset, std::vector<GenRecord>& out, int threads) {
-  out.clear();
-  if (N < 5 || N > kMaxN || preset < 1) return -1;
+int start_constellations(int N, std::vector<int>& starts) {
+  starts.clear();
+  if (N < 5 || N > kMaxN) return -1;
   const int halfN = (N + 1) / 2, N1 = N - 1, N2 = N - 2;
   // S: the set of start constellations (random access for the rotation check),
   // with its members also listed so nothing scans all 2^20 packed ijkl values.
@@ -158,13 +158,21 @@ int gen_constellations(int N, int preset, std::vector<GenRecord>& out, int threa
   for (int j = 1; j < N2; j++)      // queen in a corner (356Py:2880)
     for (int l = j + 1; l < N1; l++) add(to_ijkl(0, j, 0, l));
   // canonical forms (jasmin), distinct, in ascending packed order
-  std::vector<int> starts;
   starts.reserve(members.size());
   for (int x : members) starts.push_back(canon(x, N));
   std::sort(starts.begin(), starts.end());
   starts.erase(std::unique(starts.begin(), starts.end()), starts.end());
+  return 0;
+}
 
-  const size_t ns = starts.size();
+int expand_starts(int N, int preset, const std::vector<int>& starts, size_t s0, size_t s1,
+                  std::vector<GenRecord>& out, int threads) {
+  if (N < 5 || N > kMaxN || preset < 1) return -1;
+  if (preset < 4) return -2;   // the start constellations already hold 3-4 queens; the reference presets are 4..8
+  const int N1 = N - 1;
+  s1 = std::min(s1, starts.size());
+  if (s0 >= s1) return 0;
+  const size_t ns = s1 - s0;
   std::vector<std::vector<GenRecord>> parts(ns);
   std::atomic<size_t> next{0};
   std::atomic<int> err{0};
@@ -172,9 +180,9 @@ int gen_constellations(int N, int preset, std::vector<GenRecord>& out, int threa
     Expander e;
     e.N = N; e.preset = preset; e.board_mask = (1ull << N) - 1;
     for (;;) {
-      const size_t s = next.fetch_add(1);
-      if (s >= ns) break;
-      const int sc = starts[s];
+      const size_t q = next.fetch_add(1);
+      if (q >= ns) break;
+      const int sc = starts[s0 + q];
       const int i = geti(sc), j = getj(sc), k = getk(sc), l = getl(sc);
       if (l < 1) { err = 1; break; }
       const uint64_t L = 1ull << N1, Lj = L >> j, Li = L >> i, Ll = L >> l;
@@ -182,7 +190,7 @@ int gen_constellations(int N, int preset, std::vector<GenRecord>& out, int threa
       const uint64_t rd = (L >> (i + 1)) | (1ull << (l - 1));
       const uint64_t col = 1 | L | Li | Lj;
       e.cache.clear(); e.sigs.clear();
-      e.k = k; e.l = l; e.out = &parts[s]; e.base = (uint32_t)to_ijkl(i, j, k, l);
+      e.k = k; e.l = l; e.out = &parts[q]; e.base = (uint32_t)to_ijkl(i, j, k, l);
       e.cached(ld, rd, col, 1, (j == N1) ? 3 : 4, Lj | Ll, Lj | (1ull << k));
       if (e.err) { err = 1; break; }
     }
@@ -196,11 +204,20 @@ int gen_constellations(int N, int preset, std::vector<GenRecord>& out, int threa
     for (auto& t : th) t.join();
   }
   if (err) return -2;
-  size_t total = 0;
+  size_t total = out.size();
   for (auto& p : parts) total += p.size();
   out.reserve(total);
   for (auto& p : parts) out.insert(out.end(), p.begin(), p.end());
   return 0;
+}
+
+int gen_constellations(int N, int preset, std::vector<GenRecord>& out, int threads) {
+  out.clear();
+  if (N < 5 || N > kMaxN || preset < 1) return -1;
+  if (preset < 4) return -2;
+  std::vector<int> starts;
+  if (int s = start_constellations(N, starts)) return s;
+  return expand_starts(N, preset, starts, 0, starts.size(), out, threads);
 }
 
 // ---------------------------------------------------------------------------

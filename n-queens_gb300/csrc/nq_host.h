@@ -28,6 +28,14 @@ struct HostTask {
 // deep for N).  threads <= 0: all hardware threads.
 int gen_constellations(int N, int preset, std::vector<GenRecord>& out, int threads);
 
+// The same in two parts, for generating a large board chunk by chunk with
+// bounded host memory: the canonical start constellations (packed ijkl,
+// ascending; cheap), then the records of starts[s0..s1) appended to `out` in
+// start order (the expansion runs on `threads` host threads).
+int start_constellations(int N, std::vector<int>& starts);
+int expand_starts(int N, int preset, const std::vector<int>& starts, size_t s0, size_t s1,
+                  std::vector<GenRecord>& out, int threads);
+
 // Tasks whose counts sum to the number of N-queens solutions containing the
 // k pre-placed queens (rows[q], cols[q]); no symmetry weight.  Returns 0 with
 // tasks appended, 1 when the count is 0 without any task (attacking queens or

@@ -13,6 +13,7 @@ constexpr uint32_t DERR_SHIFT = 1u;      // a record needs a negative shift (ref
 constexpr uint32_t DERR_DEPTH = 2u;      // a task's schedule is deeper than the launch's stack
 constexpr uint32_t DERR_NOTERM = 4u;     // a schedule never reaches a base frame
 constexpr uint32_t DERR_BADN = 8u;       // N outside 6..27 in a task
+constexpr uint32_t DERR_FORMAT = 16u;    // a schedule op does not fit the compact word's fields
 
 // Prepared task arrays (structure of arrays, one entry per task).
 struct TaskArrays {
@@ -29,7 +30,7 @@ struct DfsLaunch {
   const uint2* sinfo = nullptr;         // ... and {task, depth}; nullptr: the queue holds tasks
   int64_t m = 0;                        // queue length
   const uint32_t* order = nullptr;      // optional queue order (task index per slot)
-  unsigned int* cursor = nullptr;       // queue cursor (device, zeroed before launch)
+  unsigned long long* cursor = nullptr; // queue cursor (device, zeroed before launch; 64-bit, so it never wraps)
   unsigned long long* job_totals = nullptr;  // weighted totals, slot (job id - job_base) (device)
   uint32_t job_base = 0;
   unsigned long long* per_task = nullptr;    // optional weighted count per task (device)
@@ -56,6 +57,12 @@ cudaError_t launch_dfs(const DfsLaunch& L, cudaStream_t st);
 cudaError_t launch_split(int pass, int D, int64_t t0, int64_t m, const TaskArrays& ta, uint32_t* nsub, uint4* sroot,
                          uint2* sinfo, unsigned long long* ctr, unsigned long long* per_task,
                          unsigned long long* job_totals, uint32_t job_base, cudaStream_t st);
+
+// Queue order, largest estimated subtree first: order[0..m) receives the queue
+// indices (subtasks when sinfo is set, else tasks); keys: m bytes of scratch,
+// hist_offs: 512 u32 of scratch.
+cudaError_t launch_order(int64_t m, const uint4* sroot, const uint2* sinfo, const TaskArrays& ta, uint8_t* keys,
+                         unsigned int* hist_offs, uint32_t* order, cudaStream_t st);
 
 // Largest block count per SM for a given stack depth (occupancy query).
 int dfs_blocks_per_sm(bool wide, int block, int maxt);

@@ -14,9 +14,12 @@
 //   expands exactly one candidate queen, so lanes stay converged on the same
 //   short instruction sequence whatever their task, depth or SQ* variant:
 //   the variant lives in the schedule word read from shared memory, not in
-//   control flow.  The current frame is in registers; saved frames (only
-//   those with candidates left, as the reference's packed stack) sit in
-//   shared memory, interleaved by lane so every access is conflict-free.
+//   control flow; the word is laid out so the child row takes two funnel
+//   shifts and no field extraction (nq_common.cuh).  The current frame is in
+//   registers; saved frames (only those with candidates left, as the
+//   reference's packed stack) sit in shared memory, interleaved by lane so
+//   every access is conflict-free, above a sentinel frame that leaves a
+//   finished lane with no free column.
 //   Counts are summed per lane in u64 and flushed per job with one atomicAdd
 //   per warp (shuffle tree) at exit or per task when the job id changes.
 #include <type_traits>
@@ -81,9 +84,15 @@ __device__ __forceinline__ int prepare_one(int N, const uint4* __restrict__ rec,
   info[t] = make_uint2(info_pack(Tw, (uint32_t)wexp, root_count, (uint32_t)N, status), job);
   if (T >= 0) {
     typename WordT<WIDE>::type* s = sched + t * sw;
+    bool fits = true;
     for (int d = 0; d <= T; d++) {
       if constexpr (WIDE) s[d] = make_uint2(pack_wide_x(ops[d]), ops[d].ra);
-      else s[d] = pack_compact(ops[d]);
+      else { fits = fits && compact_fits(ops[d], N); s[d] = pack_compact(ops[d]); }
+    }
+    if (!fits) {                      // never seen (N=6..21, presets 4-7): fail loudly rather than miscount
+      atomicOr(err, DERR_FORMAT);
+      info[t] = make_uint2(info_pack(INFO_NO_DFS, (uint32_t)wexp, 0u, (uint32_t)N, TS_FORMAT), job);
+      return -1;
     }
   }
   return T;
@@ -122,19 +131,14 @@ cudaError_t launch_prepare(int N, int64_t m, const uint4* records, const TaskArr
 // Schedule word decoding shared by the split and DFS kernels
 // ---------------------------------------------------------------------------
 struct Dec { uint32_t s, la, ra, fc, term, tall; };
-__device__ __forceinline__ Dec decode(uint32_t w) {
-  return Dec{w >> C_SSHIFT, w & C_LA, w & C_RA, w & C_FC, w & C_TERM, w & C_TALL};
+// compact word of depth k of a task of board N and terminal depth T
+__device__ __forceinline__ Dec decode(uint32_t w, uint32_t N, uint32_t k, uint32_t T) {
+  const Op o = unpack_compact(w, (int)N, k == T);
+  return Dec{o.s, o.la, o.ra, o.fc, o.term, o.tall};
 }
-__device__ __forceinline__ Dec decode(uint2 w) {
+__device__ __forceinline__ Dec decode(uint2 w, uint32_t, uint32_t, uint32_t) {
   return Dec{(w.x >> W_SSHIFT) & 7u, w.x & W_LA, w.y, w.x & W_FC, w.x & W_TERM, w.x & W_TALL};
 }
-
-// The same decode with the shift field taken by a multiply-high, which issues
-// on the FMA pipe instead of the integer ALU pipe (the DFS step's binding pipe).
-__device__ __forceinline__ Dec decode_fma(uint32_t w) {
-  return Dec{__umulhi(w, 1u << (32 - C_SSHIFT)), w & C_LA, w & C_RA, w & C_FC, w & C_TERM, w & C_TALL};
-}
-__device__ __forceinline__ Dec decode_fma(uint2 w) { return decode(w); }
 
 // ---------------------------------------------------------------------------
 // split: expand every task to depth D (1..3) so the DFS queue holds many
@@ -198,7 +202,7 @@ __global__ void __launch_bounds__(256) split_kernel(int pass, int64_t t0, int64_
         if (f.w == 0u) { --k; continue; }
         const uint32_t bit = f.w & (0u - f.w);
         f.w ^= bit;
-        const Dec o = decode(w[k]);
+        const Dec o = decode(w[k], info_N(in.x), (uint32_t)k, T);
         const uint32_t nld = ((f.x | bit) << o.s) | o.la;
         const uint32_t nrd = ((f.y | bit) >> o.s) | o.ra;
         const uint32_t ncol = f.z | bit;
@@ -262,6 +266,88 @@ cudaError_t launch_split(int pass, int D, int64_t t0, int64_t m, const TaskArray
 }
 
 // ---------------------------------------------------------------------------
+// queue order: largest estimated subtree first.  The reference reorders its
+// task list by a hand-tuned cost score before launching (chunkshape148 score
+// key and mark-distance risk table, 356Py_savesp_narrow.py:4310-4372 and
+// 3646-3748) so long tasks start early instead of forming the tail.  Here the
+// estimate is the frame's candidate count plus the free squares of the next
+// six rows ignoring later placements, popc(bm & ~((ld << k) | (rd >> k) | col))
+// for k = 1..6: at N=16 (split depth 2) its rank correlation with the true
+// subtree size is 0.73.  The keys (0..255) are sorted on the device by a
+// counting sort: histogram, a descending exclusive scan, and a scatter with
+// one atomic per warp and key.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t cost_key(const uint4 f, uint32_t bm) {
+  uint32_t k = __popc(f.w);
+#pragma unroll
+  for (int s = 1; s <= 6; s++) k += __popc(bm & ~((f.x << s) | (f.y >> s) | f.z));
+  return k < 255u ? k : 255u;
+}
+
+__global__ void __launch_bounds__(256) order_hist_kernel(int64_t m, const uint4* __restrict__ sroot,
+                                                         const uint2* __restrict__ sinfo,
+                                                         const uint4* __restrict__ root, const uint2* __restrict__ info,
+                                                         uint8_t* __restrict__ keys, unsigned int* hist) {
+  __shared__ unsigned int h[256];
+  h[threadIdx.x] = 0;
+  __syncthreads();
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < m) {
+    const uint32_t task = sinfo ? sinfo[q].x : (uint32_t)q;
+    const uint4 f = sinfo ? sroot[q] : root[q];
+    const uint32_t key = cost_key(f, (1u << info_N(info[task].x)) - 1u);
+    keys[q] = (uint8_t)key;
+    atomicAdd(&h[key], 1u);
+  }
+  __syncthreads();
+  if (h[threadIdx.x]) atomicAdd(&hist[threadIdx.x], h[threadIdx.x]);
+}
+
+// offs[k] = number of items with a larger key (one block of 256 threads)
+__global__ void __launch_bounds__(256) order_scan_kernel(const unsigned int* __restrict__ hist,
+                                                         unsigned int* __restrict__ offs) {
+  __shared__ unsigned int v[256];
+  const int t = threadIdx.x;
+  v[t] = hist[255 - t];                // descending key order
+  __syncthreads();
+  for (int o = 1; o < 256; o <<= 1) {   // inclusive scan
+    const unsigned int x = (t >= o) ? v[t - o] : 0u;
+    __syncthreads();
+    v[t] += x;
+    __syncthreads();
+  }
+  offs[255 - t] = v[t] - hist[255 - t];
+}
+
+__global__ void __launch_bounds__(256) order_scatter_kernel(int64_t m, const uint8_t* __restrict__ keys,
+                                                            unsigned int* offs, uint32_t* __restrict__ order) {
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const unsigned lane = threadIdx.x & 31u;
+  const bool active = q < m;
+  const unsigned live = __ballot_sync(FULL, active);
+  if (!active) return;
+  const uint32_t key = keys[q];
+  const unsigned same = __match_any_sync(live, key);      // lanes of this warp with the same key
+  const int leader = __ffs(same) - 1;
+  unsigned base = 0;
+  if ((int)lane == leader) base = atomicAdd(&offs[key], (unsigned)__popc(same));
+  base = __shfl_sync(same, base, leader);
+  order[base + __popc(same & ((1u << lane) - 1u))] = (uint32_t)q;
+}
+
+cudaError_t launch_order(int64_t m, const uint4* sroot, const uint2* sinfo, const TaskArrays& ta, uint8_t* keys,
+                         unsigned int* hist_offs, uint32_t* order, cudaStream_t st) {
+  if (m <= 0) return cudaSuccess;
+  const unsigned G = (unsigned)((m + 255) / 256);
+  cudaError_t e = cudaMemsetAsync(hist_offs, 0, 256 * sizeof(unsigned int), st);
+  if (e != cudaSuccess) return e;
+  order_hist_kernel<<<G, 256, 0, st>>>(m, sroot, sinfo, ta.root, ta.info, keys, hist_offs);
+  order_scan_kernel<<<1, 256, 0, st>>>(hist_offs, hist_offs + 256);
+  order_scatter_kernel<<<G, 256, 0, st>>>(m, keys, hist_offs + 256, order);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // DFS
 // ---------------------------------------------------------------------------
 struct DfsArgs {
@@ -273,7 +359,7 @@ struct DfsArgs {
   const uint2* sinfo;
   int64_t m;                  // queue length
   const uint32_t* order;
-  unsigned int* cursor;
+  unsigned long long* cursor;
   unsigned long long* job_totals;
   uint32_t job_base;
   unsigned long long* per_task;
@@ -285,8 +371,12 @@ __device__ __forceinline__ void flush_job(const DfsArgs& a, unsigned job, unsign
   if (v) atomicAdd(a.job_totals + (job - a.job_base), v);
 }
 
+// Saved frames per lane: at most one per depth 0..T'-1 above the sentinel.
+__host__ __device__ constexpr int stack_slots(int maxt) { return maxt + 1; }
+constexpr uint32_t SENT_COL = 0x07FFFFFFu;   // sentinel frame's col: every column blocked, depth 0
+
 size_t dfs_smem_bytes(bool wide, int block, int maxt) {
-  return (size_t)block * ((size_t)maxt * sizeof(uint4) + (size_t)(maxt + 1) * (wide ? 8 : 4));
+  return (size_t)block * ((size_t)stack_slots(maxt) * sizeof(uint4) + (size_t)(maxt + 1) * (wide ? 8 : 4));
 }
 
 // One lane's DFS state and its step.  Every lane runs the same predicated
@@ -295,7 +385,7 @@ size_t dfs_smem_bytes(bool wide, int block, int maxt) {
 // apply the look-ahead, then count (terminal depth) or descend.  '+' replaces
 // '|' where the bits are disjoint (a candidate is never in ld, rd or col),
 // so those adds issue on the FMA pipe as well as the ALU pipe.  Per-task
-// counts are u32 (BIG: u64, for N >= 24, where one task may pass 2^32).
+// counts are u32 (BIG: u64, where a queue item may count 2^32 solutions).
 static_assert(kMaxN <= 27, "a frame's depth is kept in col bits 27-31");
 
 // Shared-memory accesses of the step, as predicated PTX so the pop and the push
@@ -319,6 +409,8 @@ struct Lane {
   uint32_t ld = 0, rd = 0, col = 0, avail = 0, bm = 0;
   uint32_t sp = 0;      // shared address of the next free frame of this lane's stack
   uint32_t sbase = 0;   // shared address of its first frame: the stack is empty when sp == sbase
+  uint32_t tl = 0;      // terminal depth of the subtask (relative to its root)
+  uint32_t ram = 0;     // compact words: the bits where RA << s may sit (compact_ra_mask)
   typename std::conditional<BIG, unsigned long long, uint32_t>::type cnt = 0;
 
   template <int BLOCK>
@@ -334,23 +426,35 @@ struct Lane {
     const uint32_t bit = avail & (0u - avail);
     avail -= bit;
     const W w = lds_word(sch + d * (BLOCK * (uint32_t)sizeof(W)), W{});
-    const Dec o = decode_fma(w);
-    uint32_t nld;
-    if constexpr (WIDE) nld = ((ld + bit) << o.s) | o.la;
-    else nld = (ld + bit) * (o.s * (o.s - 1u) + 2u) + o.la;   // (x << s) | la: s*s - s + 2 = 1 << s for the
-                                                               // compact word's s in 1..3, la lies below bit s
-    const uint32_t nrd = ((rd + bit) >> o.s) | o.ra;
+    uint32_t nld, nrd;
+    bool term, fc, tall = false;
+    if constexpr (WIDE) {
+      const Dec o = decode(w, 0u, 0u, 0u);
+      nld = ((ld + bit) << o.s) | o.la;
+      nrd = ((rd + bit) >> o.s) | o.ra;
+      term = o.term != 0u; fc = o.fc != 0u; tall = o.tall != 0u;
+    } else {
+      // nld = (x << s) | LA in one funnel shift of the word (LA in its top s bits, s in its low 5);
+      // nrd = ((y | RA << s) >> s) = (y >> s) | RA, RA << s or-ed in from the word's bits N-1..N
+      asm("shf.l.wrap.b32 %0, %1, %2, %1;" : "=r"(nld) : "r"(w), "r"(ld + bit));
+      uint32_t y;
+      asm("lop3.b32 %0, %1, %2, %3, 0xF8;" : "=r"(y) : "r"(rd + bit), "r"(w), "r"(ram));   // a | (b & c)
+      asm("shf.r.wrap.b32 %0, %1, 0, %2;" : "=r"(nrd) : "r"(y), "r"(w));
+      term = d == tl; fc = (w & C_FC) != 0u;
+    }
     const uint32_t ncol = col + bit;
     const uint32_t free_cols = bm & ~ncol;
     const uint32_t nf = free_cols & ~(nld | nrd);
     const uint32_t ahead = free_cols & ~((nld + nld) | __umulhi(nrd, 0x80000000u));   // nrd >> 1
     // terminal depth: count the child (the SQd2B rule is LA bit 0 of the word);
-    // otherwise descend unless the child row or, with look-ahead, the row after is full
-    const bool live = act && nf != 0u;
-    bool hit = live && o.term;
-    if constexpr (WIDE) hit = hit || (act && o.term && o.tall);
+    // otherwise descend unless the child row or, with look-ahead, the row after is full.
+    // A lane with nothing left holds the sentinel frame (no free column), so nf == 0
+    // there; only the tall rule of wide words needs the lane's activity itself.
+    const bool live = nf != 0u;
+    bool hit = live && term;
+    if constexpr (WIDE) hit = (act && live && term) || (act && term && tall);
     cnt += hit ? 1u : 0u;
-    const bool desc = live && !o.term && !(o.fc && ahead == 0u);
+    const bool desc = (WIDE ? act : true) && live && !term && !(fc && ahead == 0u);
     const uint32_t push = (desc && avail != 0u) ? 1u : 0u;
     asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %0, 0;\n\t@p st.shared.v4.u32 [%1], {%2, %3, %4, %5};\n\t}"
                  :: "r"(push), "r"(sp), "r"(ld), "r"(rd), "r"(col), "r"(avail) : "memory");
@@ -364,7 +468,7 @@ __global__ void __launch_bounds__(BLOCK) dfs_kernel(const DfsArgs a) {
   using W = typename WordT<WIDE>::type;
   extern __shared__ __align__(16) unsigned char smem[];
   uint4* stk = reinterpret_cast<uint4*>(smem) + threadIdx.x;                                   // stride BLOCK
-  W* sch = reinterpret_cast<W*>(smem + (size_t)a.maxt * BLOCK * sizeof(uint4)) + threadIdx.x;  // stride BLOCK
+  W* sch = reinterpret_cast<W*>(smem + (size_t)stack_slots(a.maxt) * BLOCK * sizeof(uint4)) + threadIdx.x;  // stride BLOCK
   const unsigned lane = threadIdx.x & 31u;
   const unsigned lt_mask = (1u << lane) - 1u;
   const W* __restrict__ gsched = reinterpret_cast<const W*>(a.sched);
@@ -393,17 +497,17 @@ __global__ void __launch_bounds__(BLOCK) dfs_kernel(const DfsArgs a) {
       const unsigned need = __ballot_sync(FULL, want);
       if (need) {
         const int leader = __ffs(need) - 1;
-        unsigned base = 0;
-        if ((int)lane == leader) base = atomicAdd(a.cursor, (unsigned)__popc(need));
+        unsigned long long base = 0;
+        if ((int)lane == leader) base = atomicAdd(a.cursor, (unsigned long long)__popc(need));
         base = __shfl_sync(FULL, base, leader);
         if (want) {
           const uint64_t slot = (uint64_t)base + (uint64_t)__popc(need & lt_mask);
           if (slot < (uint64_t)a.m) {
-            const uint32_t q = a.order ? a.order[slot] : (uint32_t)slot;
+            const uint64_t q = a.order ? (uint64_t)a.order[slot] : slot;
             uint4 r;
             uint32_t d0;
             if (a.sinfo) { const uint2 si = a.sinfo[q]; task = si.x; d0 = si.y; r = a.sroot[q]; }
-            else { task = q; d0 = 0; r = a.root[q]; }
+            else { task = (uint32_t)q; d0 = 0; r = a.root[q]; }
             const uint2 in = a.info[task];
             const uint32_t T = info_T(in.x);
             have = true;
@@ -413,14 +517,18 @@ __global__ void __launch_bounds__(BLOCK) dfs_kernel(const DfsArgs a) {
             L.bm = (1u << info_N(in.x)) - 1u;
             L.sp = L.sbase;
             if (T == INFO_NO_DFS || info_status(in.x) != TS_OK || T < d0) {
-              L.avail = 0;
+              L.avail = 0; L.col = SENT_COL;
             } else if ((int)(T - d0) > a.maxt) {    // frames at depths 0..T'-1, words 0..T'
               atomicOr(a.err, DERR_DEPTH);
-              L.avail = 0;
+              L.avail = 0; L.col = SENT_COL;
             } else {
               L.ld = r.x; L.rd = r.y; L.col = r.z & L.bm; L.avail = r.w;
+              L.tl = T - d0; L.ram = compact_ra_mask((int)info_N(in.x));
               const W* src = gsched + (size_t)task * a.sw + d0;
               for (uint32_t k = 0; k <= T - d0; k++) sch[k * BLOCK] = src[k];
+              // the sentinel under the stack: popped after the last real frame, it leaves no free column
+              stk[0] = make_uint4(0u, 0u, SENT_COL, 0u);
+              L.sp = L.sbase + BLOCK * (uint32_t)sizeof(uint4);
             }
           } else {
             exhausted = true;

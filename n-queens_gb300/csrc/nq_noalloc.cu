@@ -75,10 +75,10 @@ extern "C" int nq_exec_solutions_noalloc(int N, const nq_record* d_records, int6
   cudaStream_t st = (cudaStream_t)stream;
   unsigned char* c = (unsigned char*)base;
   unsigned long long* totals = (unsigned long long*)c;
-  unsigned int* cursor = (unsigned int*)(c + 8);
-  unsigned int* err = (unsigned int*)(c + 12);
+  unsigned long long* cursor = (unsigned long long*)(c + 8);
+  unsigned int* err = (unsigned int*)(c + 16);
   // the array keeps the previous call's contents: clear what must start at zero
-  if (cudaMemsetAsync(c, 0, 16, st) != cudaSuccess) return NQ_ECUDA;
+  if (cudaMemsetAsync(c, 0, 24, st) != cudaSuccess) return NQ_ECUDA;
   if (m > 0) {
     TaskArrays ta;
     ta.root = (uint4*)(c + kCtrlBytes);
@@ -90,7 +90,7 @@ extern "C" int nq_exec_solutions_noalloc(int N, const nq_record* d_records, int6
     DfsLaunch L;
     L.tasks = ta; L.m = m; L.cursor = cursor; L.job_totals = totals;
     L.per_task = (unsigned long long*)d_solutions; L.err = err; L.maxt = maxt; L.block = 128; L.grid = 0;
-    L.big = N >= 24;
+    L.big = counts_need_u64(N, m);
     if (launch_dfs(L, st) != cudaSuccess) return NQ_ECUDA;
   }
   if (cudaMemcpyAsync(d_total, totals, 8, cudaMemcpyDeviceToDevice, st) != cudaSuccess) return NQ_ECUDA;

@@ -25,6 +25,7 @@
 
 #include "../../include/nqueens_gb300.h"
 #include "nq_common.cuh"
+#include "nq_handle.h"
 #include "nq_internal.h"
 
 namespace nq {
@@ -307,12 +308,13 @@ int build_unique_tasks(int N, int64_t min_tasks, std::vector<UConf>& confs, std:
 using namespace nq;
 
 extern "C" int nq_count_unique(nq_handle* h, int N, uint64_t* unique, uint64_t* total) {
-  if (!h || !unique || !total) return NQ_EINVAL;
-  if (N < 4 || N > kMaxN) return NQ_EINVAL;
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess) return NQ_ECUDA;
-  int sms = 0;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (!h) return NQ_EINVAL;
+  if (!unique || !total) return h->fail(NQ_EINVAL, "count_unique: null output");
+  if (N < 4 || N > kMaxN) return h->fail(NQ_EINVAL, "count_unique: N=%d outside 4..27", N);
+  // the handle's device and stream, and buffers the handle keeps between calls
+  NQ_CUDA(h, cudaSetDevice(h->device));
+  const int dev = h->device, sms = h->sms;
+  cudaStream_t st = h->stream;
   std::vector<UConf> confs;
   std::vector<UTask> tasks;
   // About 8 tasks per resident lane (the kernel keeps ~512 lanes per SM): fewer
@@ -325,47 +327,35 @@ extern "C" int nq_count_unique(nq_handle* h, int N, uint64_t* unique, uint64_t* 
   const int maxf = std::max(1, N - 2 - (int)min_row);
   constexpr int B = 128;
   const size_t smem = (size_t)B * ((size_t)maxf * sizeof(uint4) + (size_t)N * sizeof(uint32_t));
-  void *d_tasks = nullptr, *d_confs = nullptr, *d_ctl = nullptr;
-  cudaStream_t st = nullptr;
-  int status = NQ_OK;
-  unsigned long long hc[3] = {0, 0, 0};
-  uint32_t herr = 0;
-  do {
-    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) { status = NQ_ECUDA; break; }
-    if (cudaMallocAsync(&d_tasks, std::max<size_t>(1, (size_t)m * sizeof(UTask)), st) != cudaSuccess ||
-        cudaMallocAsync(&d_confs, std::max<size_t>(1, confs.size() * sizeof(UConf)), st) != cudaSuccess ||
-        cudaMallocAsync(&d_ctl, 64, st) != cudaSuccess) { status = NQ_ENOMEM; break; }
-    if (cudaMemsetAsync(d_ctl, 0, 64, st) != cudaSuccess) { status = NQ_ECUDA; break; }
-    if (m > 0 && cudaMemcpyAsync(d_tasks, tasks.data(), (size_t)m * sizeof(UTask), cudaMemcpyHostToDevice, st) != cudaSuccess) { status = NQ_ECUDA; break; }
-    if (!confs.empty() && cudaMemcpyAsync(d_confs, confs.data(), confs.size() * sizeof(UConf), cudaMemcpyHostToDevice, st) != cudaSuccess) { status = NQ_ECUDA; break; }
-    if (m > 0) {
-      int optin = 0;   // the cap is process-wide: set it to the device maximum, never to one launch's size
-      if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess ||
-          cudaFuncSetAttribute(unique_kernel<B>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) != cudaSuccess) {
-        status = NQ_ECUDA; break;
-      }
-      int per = 0;
-      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, unique_kernel<B>, B, smem) != cudaSuccess || per <= 0) { status = NQ_ECUDA; break; }
-      UArgs a;
-      a.tasks = (const UTask*)d_tasks; a.confs = (const UConf*)d_confs; a.m = m; a.N = N; a.maxf = maxf;
-      a.counts = (unsigned long long*)d_ctl; a.cursor = (unsigned int*)((char*)d_ctl + 32);
-      a.err = (unsigned int*)((char*)d_ctl + 36);
-      unique_kernel<B><<<sms * per, B, smem, st>>>(a);
-      if (cudaGetLastError() != cudaSuccess) { status = NQ_ECUDA; break; }
-    }
-    if (cudaMemcpyAsync(hc, d_ctl, 24, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-        cudaMemcpyAsync(&herr, (char*)d_ctl + 36, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-        cudaStreamSynchronize(st) != cudaSuccess) { status = NQ_ECUDA; break; }
-  } while (0);
-  if (st) {
-    if (d_tasks) cudaFreeAsync(d_tasks, st);
-    if (d_confs) cudaFreeAsync(d_confs, st);
-    if (d_ctl) cudaFreeAsync(d_ctl, st);
-    cudaStreamSynchronize(st);
-    cudaStreamDestroy(st);
+  NQ_CUDA(h, h->utasks.ensure(std::max<size_t>(1, (size_t)m * sizeof(UTask))));
+  NQ_CUDA(h, h->uconfs.ensure(std::max<size_t>(1, confs.size() * sizeof(UConf))));
+  NQ_CUDA(h, h->uctl.ensure(64));
+  unsigned char* ctl = (unsigned char*)h->uctl.p;
+  NQ_CUDA(h, cudaMemsetAsync(ctl, 0, 64, st));
+  if (m > 0) NQ_CUDA(h, cudaMemcpyAsync(h->utasks.p, tasks.data(), (size_t)m * sizeof(UTask), cudaMemcpyHostToDevice, st));
+  if (!confs.empty())
+    NQ_CUDA(h, cudaMemcpyAsync(h->uconfs.p, confs.data(), confs.size() * sizeof(UConf), cudaMemcpyHostToDevice, st));
+  if (m > 0) {
+    int optin = 0;   // the cap is process-wide: set it to the device maximum, never to one launch's size
+    NQ_CUDA(h, cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    NQ_CUDA(h, cudaFuncSetAttribute(unique_kernel<B>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    int per = 0;
+    NQ_CUDA(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, unique_kernel<B>, B, smem));
+    if (per <= 0) return h->fail(NQ_ECUDA, "count_unique: N=%d does not fit on an SM", N);
+    UArgs a;
+    a.tasks = (const UTask*)h->utasks.p; a.confs = (const UConf*)h->uconfs.p; a.m = m; a.N = N; a.maxf = maxf;
+    a.counts = (unsigned long long*)ctl; a.cursor = (unsigned int*)(ctl + 32);
+    a.err = (unsigned int*)(ctl + 36);
+    unique_kernel<B><<<sms * per, B, smem, st>>>(a);
+    NQ_CUDA(h, cudaGetLastError());
   }
-  if (status != NQ_OK) return status;
-  if (herr) return NQ_EINVAL;
+  // the host task vectors stay alive until the stream has consumed them (synchronised below)
+  if (int s = h->ensure_pinned(64)) return s;
+  NQ_CUDA(h, cudaMemcpyAsync(h->h_ctrl, ctl, 64, cudaMemcpyDeviceToHost, st));
+  NQ_CUDA(h, cudaStreamSynchronize(st));
+  const unsigned long long* hc = (const unsigned long long*)h->h_ctrl;
+  const uint32_t herr = ((const uint32_t*)h->h_ctrl)[9];
+  if (herr) return h->fail(NQ_EINVAL, "count_unique: device error word %u", herr);
   *unique = hc[0] + hc[1] + hc[2];
   *total = 2 * hc[0] + 4 * hc[1] + 8 * hc[2];
   return NQ_OK;

@@ -61,8 +61,11 @@ SIGNATURES = {
     "nq_destroy": (None, [_vp]),
     "nq_last_error": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_size_t]),
     "nq_device_name": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_size_t]),
+    "nq_device_sms": (ctypes.c_int, [_vp, _ip]),
     "nq_set_config": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "nq_get_config": (ctypes.c_int, [_vp, _ip, _ip, _ip]),
+    "nq_set_queue_order": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "nq_get_queue_order": (ctypes.c_int, [_vp, _ip]),
     "nq_preset_for": (ctypes.c_int, [ctypes.c_int]),
     "nq_gen_constellations": (ctypes.c_int64, [ctypes.c_int, ctypes.c_int, _vp, ctypes.c_int64]),
     "nq_gen_constellations_wide": (ctypes.c_int64, [ctypes.c_int, ctypes.c_int, _u64p, _u64p, _u64p, _u32p,
@@ -75,6 +78,8 @@ SIGNATURES = {
     "nq_last_run_info": (ctypes.c_int, [_vp, _ip, ctypes.POINTER(ctypes.c_int64)]),
     "nq_last_kernel_ms": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
     "nq_count": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _u64p]),
+    "nq_set_chunk_records": (ctypes.c_int, [_vp, ctypes.c_int64]),
+    "nq_last_count_info": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]),
     "nq_count_unique": (ctypes.c_int, [_vp, ctypes.c_int, _u64p, _u64p]),
     "nq_count_completions": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _ip, _ip, _u64p]),
     "nq_debug_task_schedule": (ctypes.c_int, [ctypes.c_int, nq_record, _u32p, _u32p, _u32p, ctypes.c_int]),
@@ -88,6 +93,7 @@ SIGNATURES = {
     "nq_batch_resident_blocks": (ctypes.c_int, [_vp, _ip]),
     "nq_tune": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _ip, _ip, ctypes.POINTER(ctypes.c_float)]),
     "nq_batch_device_bytes": (ctypes.c_int64, [_vp]),
+    "nq_job_device_bytes": (ctypes.c_int64, [ctypes.POINTER(nq_job), ctypes.c_int, ctypes.c_int]),
     "nq_batch_h2d_bytes": (ctypes.c_int64, [_vp]),
     "nq_batch_run": (ctypes.c_int, [_vp, ctypes.c_int, _u64p]),
     "nq_batch_run_plain": (ctypes.c_int, [_vp, _u64p]),

@@ -16,7 +16,13 @@ profiles/ captures a warm kernel.
 
 --tasks counts one of the reference's cached task files (16-byte records,
 N taken from the file name or --n) and --write-solutions writes the
-per-record counts as the reference's 40-byte solutions_*_v2.bin cache.
+per-record counts as the reference's 40-byte solutions_*_v2.bin cache.  The
+task file holds only the low 32 bits of each mask, so the written cache is
+keyed by those: it is found again by a reference run that also loads its
+constellations from the task file, not by one that generates them afresh
+with full-width masks.  For full-width keys use --n with --regenerate, which
+generates the board's constellations (nqueens.gen_records_wide) instead of
+reading a task file.
 """
 from __future__ import annotations
 
@@ -40,26 +46,46 @@ def _count_task_file(a) -> int:
     import os
     import re
 
-    import numpy as np
-
     from . import formats
     m = re.search(r"_N(\d+)_", os.path.basename(a.tasks))
     N = a.n or (int(m.group(1)) if m else 0)
     if not 6 <= N <= 27:
         print(f"{a.tasks}: give the board size with --n (6..27)", file=sys.stderr)
         return 2
-    recs = formats.load_tasks(a.tasks)
+    return _count_records(a, N, formats.load_tasks(a.tasks), None, a.tasks)
+
+
+def _count_records(a, N, recs, wide, name) -> int:
+    import numpy as np
+
+    from . import formats
     eng = Engine(a.device, block=a.block, split=a.split)
-    t0 = dt.datetime.now()
-    total, sol = eng.exec_records(N, recs, want_solutions=bool(a.write_solutions))
-    el = dt.datetime.now() - t0
+    try:
+        t0 = dt.datetime.now()
+        total, sol = eng.exec_records(N, recs, want_solutions=bool(a.write_solutions))
+        el = dt.datetime.now() - t0
+    finally:
+        eng.close()
     status = "ok" if N < len(EXPECTED) and EXPECTED[N] == total else "(no known answer for this task set)"
-    print(f"{a.tasks}: N={N} records={len(recs)} total={total} {_fmt(el)} {status}")
+    print(f"{name}: N={N} records={len(recs)} total={total} {_fmt(el)} {status}")
     if a.write_solutions:
-        formats.save_solutions(a.write_solutions, recs["ld"].astype(np.uint64), recs["rd"].astype(np.uint64),
-                               recs["col"].astype(np.uint64), recs["startijkl"].astype(np.uint64), sol)
-    eng.close()
+        if wide is not None:                  # full-width masks, as the reference's fresh constellations carry
+            ld, rd, col, sijkl = wide
+        else:                                 # the task file's 32-bit masks
+            ld, rd, col = (recs[k].astype(np.uint64) for k in ("ld", "rd", "col"))
+            sijkl = recs["startijkl"]
+        formats.save_solutions(a.write_solutions, ld, rd, col, sijkl.astype(np.uint64), sol)
     return 0
+
+
+def _count_regenerated(a) -> int:
+    from .engine import gen_records, gen_records_wide
+    N = a.n
+    if not 6 <= N <= 27:
+        print("--regenerate needs --n (6..27)", file=sys.stderr)
+        return 2
+    preset = a.preset or None
+    return _count_records(a, N, gen_records(N, preset), gen_records_wide(N, preset), f"N={N} generated")
 
 
 def main(argv=None) -> int:
@@ -73,23 +99,31 @@ def main(argv=None) -> int:
     ap.add_argument("--unique", action="store_true", help="also count unique solutions (symmetry method)")
     ap.add_argument("--tasks", help="count a reference task file constellations_N{N}_{P}.bin")
     ap.add_argument("--n", type=int, default=0, help="board size of --tasks when its name does not give it")
-    ap.add_argument("--write-solutions", help="with --tasks: write the per-record counts as a v2 solutions file")
+    ap.add_argument("--write-solutions", help="with --tasks or --regenerate: write the per-record counts as a v2 "
+                                              "solutions file")
+    ap.add_argument("--regenerate", action="store_true",
+                    help="with --n: generate the constellations (full-width masks) instead of reading --tasks")
+    ap.add_argument("--preset", type=int, default=0, help="with --regenerate: preset queens (0: the dynamic preset)")
     a = ap.parse_args(argv)
+    if a.regenerate:
+        return _count_regenerated(a)
     if a.tasks:
         return _count_task_file(a)
     eng = Engine(a.device, block=a.block, split=a.split)   # the defaults keep the autotuned table
-    print(" N:             Total           Unique         hh:mm:ss.ms")
     rc = 0
-    for N in range(a.nmin, a.nmax):
-        for _ in range(max(1, a.repeat)):
-            t0 = dt.datetime.now()
-            r = eng.count_unique(N) if a.unique and N >= 4 else eng.count(N)
-            el = dt.datetime.now() - t0
-        status = "ok" if N < len(EXPECTED) and EXPECTED[N] == r.total else f"ng({r.total}!={EXPECTED[N]})"
-        if status != "ok":
-            rc = 1
-        print(f"{N:2d}:{r.total:18d}{r.unique:17d}{_fmt(el):>21s}    {status}", flush=True)
-    eng.close()
+    try:
+        print(" N:             Total           Unique         hh:mm:ss.ms")
+        for N in range(a.nmin, a.nmax):
+            for _ in range(max(1, a.repeat)):
+                t0 = dt.datetime.now()
+                r = eng.count_unique(N) if a.unique and N >= 4 else eng.count(N)
+                el = dt.datetime.now() - t0
+            status = "ok" if N < len(EXPECTED) and EXPECTED[N] == r.total else f"ng({r.total}!={EXPECTED[N]})"
+            if status != "ok":
+                rc = 1
+            print(f"{N:2d}:{r.total:18d}{r.unique:17d}{_fmt(el):>21s}    {status}", flush=True)
+    finally:
+        eng.close()
     return rc
 
 

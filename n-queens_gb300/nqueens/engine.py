@@ -216,6 +216,25 @@ class Batch:
             pass
 
 
+_JOB_BYTES: Dict[tuple, int] = {}
+
+
+def job_device_bytes(job, sms: int, split: int = -1) -> int:
+    """Upper estimate of the device bytes a batch holding this one job takes on a GPU with `sms`
+    multiprocessors (nq_job_device_bytes: host-side sizing, no device needed).  Whole-board counts are
+    cached per (N, preset), since sizing one generates its constellations."""
+    key = ("count", job.N, job.preset, sms, split) if isinstance(job, CountJob) else None
+    if key is not None and key in _JOB_BYTES:
+        return _JOB_BYTES[key]
+    s = _job_struct(job)
+    n = int(lib().nq_job_device_bytes(ctypes.byref(s), int(sms), int(split)))
+    if n < 0:
+        _check(n, what=f"job_device_bytes(N={job.N})")
+    if key is not None:
+        _JOB_BYTES[key] = n
+    return n
+
+
 class Engine:
     """One CUDA device and stream of libnqgpu.so."""
 
@@ -260,6 +279,15 @@ class Engine:
                self._h, f"tune(N={N})")
         self._tuning = None
         return b.value, s.value, ms.value
+
+    def set_queue_order(self, mode: int) -> None:
+        """DFS queue order of single-N counts: 0 generator order, 1 largest estimated subtree first."""
+        _check(lib().nq_set_queue_order(self._h, int(mode)), self._h, "set_queue_order")
+
+    def get_queue_order(self) -> int:
+        v = ctypes.c_int()
+        _check(lib().nq_get_queue_order(self._h, ctypes.byref(v)), self._h, "get_queue_order")
+        return v.value
 
     def get_config(self) -> Tuple[int, int, int]:
         b, g, o = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
@@ -314,6 +342,16 @@ class Engine:
         _check(lib().nq_count(self._h, int(N), int(preset or 0), _lib.p64(t)), self._h, f"count(N={N})")
         return Result(total=int(t[0]))
 
+    def set_chunk_records(self, records: int) -> None:
+        """Records per chunk of count() (0: the library default); bounds the host memory of large boards."""
+        _check(lib().nq_set_chunk_records(self._h, int(records)), self._h, "set_chunk_records")
+
+    def last_count_info(self) -> Tuple[int, int]:
+        """(chunks, records) of the last count()."""
+        c, r = ctypes.c_int64(), ctypes.c_int64()
+        _check(lib().nq_last_count_info(self._h, ctypes.byref(c), ctypes.byref(r)), self._h, "last_count_info")
+        return c.value, r.value
+
     def count_unique(self, N: int) -> Result:
         """Unique and total counts by the symmetry method (07Py_bit_symmetry.py), 4 <= N <= 27."""
         u = np.zeros(1, np.uint64)
@@ -336,6 +374,15 @@ class Engine:
         v = ctypes.c_int()
         _check(lib().nq_resident_blocks(self._h, int(wide), int(maxt), ctypes.byref(v)), self._h, "resident_blocks")
         return v.value
+
+    def sms(self) -> int:
+        v = ctypes.c_int()
+        _check(lib().nq_device_sms(self._h, ctypes.byref(v)), self._h, "device_sms")
+        return v.value
+
+    def job_device_bytes(self, job) -> int:
+        """Upper estimate of the device bytes a batch of this one job takes on this GPU (nq_job_device_bytes)."""
+        return job_device_bytes(job, self.sms(), self.get_config()[2])
 
     def batch(self, jobs: Iterable) -> Batch:
         return Batch(self, list(jobs))

@@ -53,31 +53,27 @@ class _InFlight:
     large: bool = False
 
 
-# GPU milliseconds of a whole-board count on GB300 (measured with bench-style timing).
+# GPU milliseconds of a whole-board count, the starting point of each server's table: measured on
+# GB300 with bench-style timing; a server replaces an entry with the run time it measures for a
+# single-request batch of that board (exponential average), so another GPU recalibrates itself.
 _COUNT_MS = {16: 0.9, 17: 3.0, 18: 16.0, 19: 108.0, 20: 860.0, 21: 7300.0}
 
 
-def estimate_ms(job) -> float:
-    """Rough GPU time of a request: a whole board from the table above; k pre-placed
-    queens cut the unweighted search (8x the symmetric one) by about N per queen."""
+def estimate_ms(job, table: Optional[dict] = None) -> float:
+    """Rough GPU time of a request: a whole board from the table; k pre-placed queens cut the
+    unweighted search (8x the symmetric one) by about N per queen."""
     N = job.N
-    base = _COUNT_MS.get(N, 0.5 if N < 16 else 80000.0)
+    t = _COUNT_MS if table is None else table
+    base = t.get(N)
+    if base is None:   # outside the table: about 9x per board size from its nearest entry
+        near = min(t, key=lambda n: abs(n - N))
+        base = t[near] * 9.0 ** (N - near)
     if isinstance(job, CountJob):
         return base
     k = len(job.queens)
     if k == 0:
         return base * 8.0
     return base * 8.0 / float(N) ** k
-
-
-def _bytes_estimate(job) -> int:
-    """Device bytes a job's tasks are expected to take, for admission before building."""
-    N = job.N
-    if isinstance(job, CountJob) and N >= 6:
-        tasks = {13: 7731, 14: 13233, 15: 21270, 16: 33046, 17: 49207, 18: 571705, 19: 897071,
-                 20: 1369061, 21: 2025282}.get(N, 200000 if N > 21 else 4300)
-        return tasks * (16 + 8 + 8 * N + 16) * 8      # tasks + split subtasks
-    return 4096 * N * (24 + 8 * (N + 1)) * 2
 
 
 @dataclass
@@ -135,6 +131,7 @@ class Server:
         self._t0: Optional[float] = None
         self._t_last = 0.0
         self._error: Optional[BaseException] = None
+        self._count_ms = dict(_COUNT_MS)   # recalibrated from measured single-board batches
         self._thread = threading.Thread(target=self._loop, name="nqueens-server", daemon=True)
         self._thread.start()
 
@@ -151,7 +148,7 @@ class Server:
                 self._t0 = now
             r = _Request(job, f, now, self._seq)
             self._seq += 1
-            (self._pending_large if estimate_ms(job) > self.large_ms else self._pending).append(r)
+            (self._pending_large if estimate_ms(job, self._count_ms) > self.large_ms else self._pending).append(r)
             self._cv.notify()
         return f
 
@@ -204,6 +201,8 @@ class Server:
             for r, v in zip(fl.requests, out.tolist()):
                 r.t_done = now
                 r.future.set_result(int(v))
+            if fl.requests:
+                self._calibrate(fl, now - fl.requests[0].t_built)
             fl.batch.close()
             with self._cv:
                 self._inflight.remove(fl)
@@ -224,14 +223,21 @@ class Server:
             take: List[_Request] = []
             est = 0
             while queue and len(take) < (1 if large else self.max_batch_jobs):
-                e = _bytes_estimate(queue[0].job)
+                e = self._job_bytes(queue[0].job)
+                if e > self.budget:        # can never fit: fails alone, the queue moves on
+                    r = queue.popleft()
+                    r.future.set_exception(NQError(-5, f"request needs about {e} device bytes, more than the "
+                                                       f"server's budget of {self.budget}"))
+                    continue
                 if take and self._admitted + est + e > self.budget:
                     break
-                if not take and self._inflight and self._admitted + e > self.budget:
+                if not take and self._admitted + e > self.budget:
                     return False          # wait for memory to free up
                 take.append(queue.popleft())
                 take[-1].t_admit = time.perf_counter()
                 est += e
+            if not take:
+                return False
             self._building += 1          # taken off the queue, not yet in flight
         try:
             batch = Batch(self.engine, [r.job for r in take])   # host build + upload, other batches keep running
@@ -262,6 +268,18 @@ class Server:
             self._batches += 1
             self._max_inflight_seen = max(self._max_inflight_seen, len(self._inflight))
         return True
+
+    def _job_bytes(self, job) -> int:
+        """Device bytes a request will take, from the engine's host-side sizing (nq_job_device_bytes)."""
+        return int(self.engine.job_device_bytes(job))
+
+    def _calibrate(self, fl: "_InFlight", seconds: float) -> None:
+        """A batch holding one whole-board count measures that board's GPU time on this device."""
+        if len(fl.requests) == 1 and isinstance(fl.requests[0].job, CountJob):
+            N = fl.requests[0].job.N
+            ms = 1e3 * seconds
+            old = self._count_ms.get(N)
+            self._count_ms[N] = ms if old is None else 0.5 * old + 0.5 * ms
 
     def _admit(self) -> bool:
         a = self._admit_lane(True)

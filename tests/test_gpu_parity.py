@@ -90,6 +90,36 @@ def test_large_board_sample_per_record(eng, oracle_mod, N):
     assert total == int(want.sum()) > 0
 
 
+def test_headline_config_every_record(eng, oracle_mod):
+    """The benchmark's workload, N=19 at preset 6: all 897,071 records against the oracle (about half a
+    minute of oracle time on the host's cores)."""
+    import nqueens
+    recs = nqueens.gen_records(19)
+    assert len(recs) == 897071
+    total, sol = eng.exec_records(19, recs, want_solutions=True)
+    want = oracle_mod.exec_solutions(19, _o_records(oracle_mod, recs), threads=0)
+    assert int(np.count_nonzero(sol != want)) == 0
+    assert total == int(want.sum()) == oracle_mod.EXPECTED_TOTAL[19]
+
+
+def test_large_counts_per_record_low_preset(eng, oracle_mod):
+    """N=22 at preset 4: few records with large counts each (the per-lane counters are sized from a bound
+    on the count per queue item), unsplit and split, per record against the oracle."""
+    import nqueens
+    recs = nqueens.gen_records(22, 4)
+    idx = np.sort(np.random.default_rng(22).choice(len(recs), size=6, replace=False))
+    sub = np.ascontiguousarray(recs[idx])
+    want = oracle_mod.exec_solutions(22, _o_records(oracle_mod, sub), threads=0)
+    old = eng.get_config()
+    try:
+        for split in (0, 2):
+            eng.set_config(64, 0, split)
+            total, sol = eng.exec_records(22, sub, want_solutions=True)
+            assert np.array_equal(sol, want), split
+    finally:
+        eng.set_config(*old)
+
+
 def test_reference_dict_dropin(eng, oracle_mod):
     import nqueens
     _, _, cs, _ = nqueens.gen_constellations(11, set(), set(), [], 5)
@@ -284,3 +314,66 @@ def test_resumable_count_on_gpu(eng, oracle_mod, tmp_path):
     counter = lambda n, r: eng.exec_records(n, r)[0]
     assert exec_records_resumable(counter, 17, recs, p, chunk=8192, stop_after=2) is None
     assert exec_records_resumable(counter, 17, recs, p, chunk=8192) == oracle_mod.EXPECTED_TOTAL[17]
+
+
+def test_sync_waits_for_its_own_count_only(oracle_mod):
+    """nq_sync waits on the handle's last count (an event), not on the whole device: two engines count
+    device-resident records on their own streams and each collects its own total and status."""
+    torch = pytest.importorskip("torch")
+    import nqueens
+    engines = [nqueens.Engine(0), nqueens.Engine(0)]
+    try:
+        outs = []
+        for e, N in zip(engines, (16, 17)):
+            recs = nqueens.gen_records(N)
+            d_rec = torch.from_numpy(recs.view(np.uint8).copy()).cuda()
+            d_tot = torch.zeros(1, dtype=torch.int64, device="cuda")
+            s = torch.cuda.Stream()
+            e.exec_device(N, d_rec.data_ptr(), len(recs), int((recs["startijkl"] >> 20).min()), d_tot.data_ptr(), 0,
+                          s.cuda_stream)
+            outs.append((N, d_rec, d_tot, s))
+        for e, (N, _, d_tot, s) in zip(reversed(engines), reversed(outs)):
+            e.sync()
+            s.synchronize()
+            assert int(d_tot.item()) == oracle_mod.EXPECTED_TOTAL[N]
+        engines[0].sync()                      # nothing pending: waits for the handle's own stream only
+    finally:
+        for e in engines:
+            e.close()
+
+
+@pytest.mark.parametrize("N,chunk", [(12, 500), (17, 6000), (18, 100000)])
+def test_chunked_whole_board_count(oracle_mod, N, chunk):
+    """count() generates and counts the records chunk by chunk (bounded host memory for the largest boards):
+    any chunk size gives the known total, and the chunks together hold every record once."""
+    import nqueens
+    e = nqueens.Engine(0)
+    try:
+        e.set_chunk_records(chunk)
+        assert e.count(N).total == oracle_mod.EXPECTED_TOTAL[N]
+        chunks, records = e.last_count_info()
+        assert records == len(nqueens.gen_records(N))
+        assert chunks >= max(2, records // (2 * chunk))
+        e.set_chunk_records(0)
+        assert e.count(N).total == oracle_mod.EXPECTED_TOTAL[N]
+        assert e.last_count_info() == (1, records)
+    finally:
+        e.close()
+
+
+def test_queue_order_leaves_counts_unchanged(eng, oracle_mod):
+    """The DFS queue sorted largest-estimate-first on the device: the same per-record counts, split and
+    unsplit."""
+    import nqueens
+    recs = nqueens.gen_records(15)
+    want = oracle_mod.exec_solutions(15, _o_records(oracle_mod, recs))
+    old = eng.get_config()
+    try:
+        eng.set_queue_order(1)
+        for split in (0, 1, 2):
+            eng.set_config(64, 0, split)
+            total, sol = eng.exec_records(15, recs, want_solutions=True)
+            assert np.array_equal(sol, want), split
+    finally:
+        eng.set_queue_order(0)
+        eng.set_config(*old)

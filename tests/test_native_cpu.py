@@ -115,10 +115,10 @@ def replay(root, info, words, wide):
             x, ra = words[d]
             s = (x >> 24) & 7; la = x & 0xFFFFFF
             fc, term, tall = x & (1 << 27), x & (1 << 28), x & (1 << 30)
-        else:
+        else:                        # compact word: s in bits 0-4, RA << s at bits N-1..N, FC bit 28, LA on top
             w = words[d]
-            s = w >> 29; la = w & 3; ra = w & 0x01FFFFFC
-            fc, term, tall = w & (1 << 25), w & (1 << 26), w & (1 << 28)
+            s = w & 31; la = w >> (32 - s); ra = (w & (3 << (N - 1))) >> s
+            fc, term, tall = w & (1 << 28), d == T, 0
         nld = (((ld | bit) << s) & M32) | la
         nrd = ((rd | bit) >> s) | ra
         ncol = col | bit
@@ -180,8 +180,8 @@ def test_lookahead_on_every_sound_word(nq, oracle_mod, N):
             continue
         for d in range(T):
             child = words[d + 1]
-            if (child >> 29) == 1 and not (child & (1 << 28)):
-                assert words[d] & (1 << 25), (i, d, hex(words[d]), hex(child))
+            if (child & 31) == 1:    # the child steps one row (compact words are never tall)
+                assert words[d] & (1 << 28), (i, d, hex(words[d]), hex(child))
                 flagged += 1
         got, nd = replay(root, info, words, wide=False)
         assert got == int(sol[i])
@@ -203,10 +203,11 @@ def test_completion_lookahead_flags(nq):
                 assert bool(w[d][0] & (1 << 27)) == sound, (queens, d)
 
 
-@pytest.mark.parametrize("N,preset", [(n, p) for n in (8, 11, 14) for p in (4, 5, 6, 7)])
-def test_compact_words_step_one_to_three_rows(nq, oracle_mod, N, preset):
-    """Compact schedule words step 1, 2 or 3 rows and keep la below bit s: the DFS kernel forms 1 << s as
-    s*s - s + 2 and adds la instead of or-ing it, both exact only under these bounds."""
+@pytest.mark.parametrize("N,preset", [(n, p) for n in (8, 11, 14, 17) for p in (4, 5, 6, 7)])
+def test_compact_word_fields_do_not_overlap(nq, oracle_mod, N, preset):
+    """Compact schedule words step 1, 2 or 3 rows (bits 0-4), keep RA << s inside bits N-1..N and LA in the
+    top s bits, clear of the look-ahead flag (bit 28): the DFS kernel's two funnel shifts read the fields in
+    place, exact only under these bounds (the prepare kernel rejects a task whose op would not fit)."""
     try:
         o = oracle_mod.gen_constellations(N, preset)
     except ValueError:
@@ -214,13 +215,49 @@ def test_compact_words_step_one_to_three_rows(nq, oracle_mod, N, preset):
     rec = np.zeros(len(o), nq.RECORD_DTYPE)
     rec["ld"] = o.ld & M32; rec["rd"] = o.rd & M32; rec["col"] = o.col & M32; rec["startijkl"] = o.startijkl
     seen = set()
-    for i in range(len(o)):
+    ram = 3 << (N - 1)
+    for i in range(0, len(o), max(1, len(o) // 4000)):
         _, info, words = schedule_of(rec[i], N)
         for w in words:
-            s = w >> 29
-            assert 1 <= s <= 3 and (w & 3) < (1 << s), (i, hex(w))
+            s = w & 31
+            assert 1 <= s <= 3, (i, hex(w))
+            la_region = (M32 >> (32 - s)) << (32 - s)
+            middle = w & ~31 & ~(1 << 28) & ~la_region & M32
+            assert middle & ~ram == 0, (i, hex(w))          # RA << s only at bits N-1..N
             seen.add(s)
     assert not seen or 1 in seen
+
+
+def _funnel_l(lo, hi, n):
+    n &= 31
+    return ((((hi << 32) | lo) << n) >> 32) & M32
+
+
+def _funnel_r(lo, hi, n):
+    n &= 31
+    return (((hi << 32) | lo) >> n) & M32
+
+
+@pytest.mark.parametrize("N", [9, 13, 16])
+def test_funnel_shift_child_masks(nq, oracle_mod, N):
+    """The DFS kernel's child rows from two funnel shifts of the compact word equal the reference's
+    ((ld | bit) << s) | LA and ((rd | bit) >> s) | RA, for masks with garbage above the board in ld and
+    high bits in rd (both occur: ld's shifted-out queens, rd's pre-loaded diagonals)."""
+    o = oracle_mod.gen_constellations(N, 5)
+    rec = np.zeros(len(o), nq.RECORD_DTYPE)
+    rec["ld"] = o.ld & M32; rec["rd"] = o.rd & M32; rec["col"] = o.col & M32; rec["startijkl"] = o.startijkl
+    rng = np.random.default_rng(N)
+    ram = 3 << (N - 1)
+    checked = 0
+    for i in range(0, len(o), max(1, len(o) // 500)):
+        _, info, words = schedule_of(rec[i], N)
+        for w in words:
+            s = w & 31; la = w >> (32 - s); ra = (w & ram) >> s
+            for x, y in rng.integers(0, 1 << 32, size=(8, 2), dtype=np.uint64).tolist():
+                assert _funnel_l(w, x, w) == ((x << s) & M32) | la
+                assert _funnel_r(y | (w & ram), 0, w) == (y >> s) | ra
+                checked += 1
+    assert checked > 0
 
 
 def completion_tasks(N, queens, min_tasks=64):

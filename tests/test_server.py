@@ -43,16 +43,34 @@ def test_server_results_exact_and_same_as_alone(oracle_mod, share_gpu, max_infli
 
 
 def test_server_small_budget_still_exact(oracle_mod):
-    """A budget smaller than one batch admits one batch at a time; results stay exact."""
+    """A budget that holds only the largest single request admits one request at a time (the budget is a hard
+    limit: requests are sized before they are built); results stay exact."""
     import nqueens
     from nqueens.server import Server, random_completion_queries
     jobs = random_completion_queries(20, seed=3, N_range=(10, 14), k_range=(1, 3))
-    with Server(budget_bytes=1, max_inflight=3, max_batch_jobs=4) as srv:
+    with Server(max_inflight=3, max_batch_jobs=4) as srv:
+        srv.budget = max(srv._job_bytes(j) for j in jobs)
         futs = [srv.submit(j) for j in jobs]
         srv.drain(120)
         got = [f.result(timeout=10) for f in futs]
         assert srv.stats().max_inflight_seen == 1
     assert got == [_oracle_answer(oracle_mod, j) for j in jobs]
+
+
+def test_server_request_beyond_the_budget_fails_alone(oracle_mod):
+    """A request whose estimated device bytes exceed the whole budget fails with NQ_ENOMEM and is never
+    built; the requests around it are served."""
+    import nqueens
+    from nqueens.server import Server
+    with Server(max_inflight=3, max_batch_jobs=4) as srv:
+        small, big = nqueens.CountJob(10), nqueens.CountJob(19)
+        srv.budget = srv._job_bytes(small) * 4
+        f_small, f_big = srv.submit(small), srv.submit(big)
+        srv.drain(120)
+        assert f_small.result(timeout=10) == 724
+        with pytest.raises(nqueens.NQError) as e:
+            f_big.result(timeout=10)
+        assert e.value.status == -5
 
 
 def test_server_rejects_bad_request():

@@ -59,6 +59,18 @@ class FakeBatch:
         pass
 
 
+class FakeEngine:
+    """Stands in for engine.Engine in the server: the host-side sizing call only."""
+
+    def __init__(self, real_sizing=False):
+        self.real_sizing = real_sizing
+
+    def job_device_bytes(self, job):
+        if self.real_sizing:                 # the library's host-side sizing, as on a GB300 (152 SMs)
+            return nqueens.engine.job_device_bytes(job, 152)
+        return FakeBatch.bytes_per_job
+
+
 @pytest.fixture
 def fake(monkeypatch, oracle_mod):
     FakeBatch.created = []
@@ -70,7 +82,7 @@ def fake(monkeypatch, oracle_mod):
 
 
 def _serve(jobs, **kw):
-    with srv_mod.Server(engine=object(), poll_us=100, **kw) as s:
+    with srv_mod.Server(engine=FakeEngine(), poll_us=100, **kw) as s:
         futs = [s.submit(j) for j in jobs]
         s.drain(60)
         return [f.result() for f in futs], s.stats()
@@ -121,7 +133,7 @@ def test_batches_overlap_within_the_budget(fake):
 
 def test_bad_request_fails_alone(fake):
     jobs = [nqueens.CountJob(8), nqueens.CompletionJob(8, [(9, 0)]), nqueens.CountJob(10)]
-    with srv_mod.Server(engine=object(), poll_us=100, max_batch_jobs=8) as s:
+    with srv_mod.Server(engine=FakeEngine(), poll_us=100, max_batch_jobs=8) as s:
         futs = [s.submit(j) for j in jobs]
         s.drain(60)
         assert futs[0].result() == 92 and futs[2].result() == 724
@@ -131,7 +143,7 @@ def test_bad_request_fails_alone(fake):
 
 def test_drain_times_out_when_a_batch_never_finishes(fake):
     fake.never_finish = True
-    s = srv_mod.Server(engine=object(), poll_us=100)
+    s = srv_mod.Server(engine=FakeEngine(), poll_us=100)
     try:
         s.submit(nqueens.CountJob(8))
         with pytest.raises(TimeoutError):
@@ -142,6 +154,45 @@ def test_drain_times_out_when_a_batch_never_finishes(fake):
 
 
 def test_submit_rejects_other_objects(fake):
-    with srv_mod.Server(engine=object(), poll_us=100) as s:
+    with srv_mod.Server(engine=FakeEngine(), poll_us=100) as s:
         with pytest.raises(TypeError):
             s.submit((8, []))
+
+
+def test_request_larger_than_the_budget_fails_alone(fake):
+    """Admission sizes each request before building it (nq_job_device_bytes): a whole N=22 board
+    (28.7 M records at preset 7, several GB) cannot fit a 1 GiB budget and fails with NQ_ENOMEM,
+    while the small requests around it are served."""
+    big = nqueens.engine.job_device_bytes(nqueens.CountJob(22), 152)
+    assert big > 4 << 30
+    jobs = [nqueens.CountJob(8), nqueens.CountJob(22), nqueens.CountJob(10)]
+    with srv_mod.Server(engine=FakeEngine(real_sizing=True), poll_us=100, budget_bytes=1 << 30) as s:
+        futs = [s.submit(j) for j in jobs]
+        s.drain(60)
+        assert futs[0].result() == 92 and futs[2].result() == 724
+        with pytest.raises(NQError) as e:
+            futs[1].result()
+        assert e.value.status == -5
+    assert all(not any(j.N == 22 for j in b.jobs) for b in fake.created)   # never built
+
+
+def test_real_sizes_cover_every_board():
+    """The sizing call covers every board (the old fixed table stopped at N=21): its upper estimate holds
+    each task's record, root, info and schedule plus the split queue, so it grows with N at a fixed split
+    depth, and a forced split depth raises it."""
+    by_n = {n: nqueens.engine.job_device_bytes(nqueens.CountJob(n), 152) for n in (10, 17, 19, 20, 21, 22)}
+    assert by_n[17] < by_n[19] < by_n[20] < by_n[21] < by_n[22]
+    assert by_n[10] < by_n[17]
+    assert by_n[19] > 897071 * (16 + 16 + 8)            # N=19: records + roots + info at least
+    assert nqueens.engine.job_device_bytes(nqueens.CountJob(19), 152, 2) > by_n[19]
+    c = nqueens.engine.job_device_bytes(nqueens.CompletionJob(18, [(0, 3), (5, 7)]), 152)
+    assert 0 < c < by_n[19]
+
+
+def test_timing_table_recalibrates_from_measured_batches(fake):
+    fake.delay_s = 0.05
+    with srv_mod.Server(engine=FakeEngine(), poll_us=100) as s:
+        assert s._count_ms[16] == srv_mod._COUNT_MS[16]
+        s.submit(nqueens.CountJob(16)).result(timeout=30)
+        s.drain(30)
+        assert s._count_ms[16] > 10 * srv_mod._COUNT_MS[16]   # the fake's 50 ms run replaced the GB300 0.9 ms

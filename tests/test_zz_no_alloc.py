@@ -41,15 +41,21 @@ def test_noalloc_matches_regular_entry_point_twice(N):
     assert m <= MAX_RECORDS
     start_min = int((recs["startijkl"] >> 20).min())
     d_rec = torch.from_numpy(recs.view(np.uint8).copy()).cuda()
+    d_total = torch.empty(1, dtype=torch.int64, device="cuda")
+    d_sol = torch.empty(m, dtype=torch.int64, device="cuda")
     s = torch.cuda.Stream()
-    for call in range(2):   # two calls in a row share (and must clear) the same scratch
-        d_total = torch.full((1,), -1, dtype=torch.int64, device="cuda")
-        d_sol = torch.full((m,), -1, dtype=torch.int64, device="cuda")
+    free_after = []
+    for call in range(3):   # calls in a row share (and must clear) the same scratch
+        d_total.fill_(-1)
+        d_sol.fill_(-1)
         torch.cuda.synchronize()
         st = _noalloc(L, N, d_rec.data_ptr(), m, start_min, d_sol.data_ptr(), d_total.data_ptr(), s.cuda_stream)
         assert st == 0, (call, st)
+        free_after.append(torch.cuda.mem_get_info()[0])   # the device's free bytes (cudaMemGetInfo)
         assert int(d_total.item()) == want_total, call
         assert np.array_equal(d_sol.cpu().numpy().view(np.uint64), want_sol), call
+    # after the first call (which may load the array and kernels), calls take no device memory
+    assert free_after[1] == free_after[2] == free_after[0], free_after
 
 
 def test_noalloc_total_only_and_limits():
