@@ -509,23 +509,29 @@ int nq_count(nq_handle* h, int N, int preset, uint64_t* total) {
   size_t next = 0;
   double per_start = 0.0;                  // records per start constellation seen so far
   std::vector<GenRecord> g;
+  // Blocks of starts are expanded and packed into 16-byte records at once, so the
+  // 32-byte generator records of at most an eighth of a chunk are alive at a time.
   auto gen_chunk = [&](std::vector<nq_record>& out) -> int {
     out.clear();
-    g.clear();
-    while (next < starts.size() && (int64_t)g.size() < chunk) {
-      const double want = (double)(chunk - (int64_t)g.size());
+    if (per_start > 0.0)   // expected size of this chunk, so the vector does not double past it
+      out.reserve((size_t)std::min((double)(chunk + chunk / 8), per_start * (double)(starts.size() - next) + 1024.0));
+    while (next < starts.size() && (int64_t)out.size() < chunk) {
+      const double want = std::min((double)(chunk - (int64_t)out.size()), (double)chunk / 8.0);
       const size_t take = per_start > 0.0 ? (size_t)std::max(1.0, want / per_start) : (size_t)16;
       const size_t s1 = std::min(starts.size(), next + take);
-      const size_t before = g.size();
+      g.clear();
       const int e = expand_starts(N, p, starts, next, s1, g, 0);
       if (e == -1) return h->fail(NQ_EINVAL, "generator: bad arguments N=%d preset=%d", N, p);
       if (e == -2) return h->fail(NQ_EPRESET, "generator: preset %d too deep for N=%d", p, N);
-      per_start = 0.5 * per_start + 0.5 * (double)(g.size() - before) / (double)(s1 - next);
+      per_start = 0.5 * per_start + 0.5 * (double)g.size() / (double)(s1 - next);
       if (per_start <= 0.0) per_start = 0.25;
       next = s1;
+      const size_t o = out.size();
+      out.resize(o + g.size());
+      for (size_t i = 0; i < g.size(); i++)
+        out[o + i] = nq_record{(uint32_t)g[i].ld, (uint32_t)g[i].rd, (uint32_t)g[i].col, g[i].startijkl};
     }
-    out.resize(g.size());
-    for (size_t i = 0; i < g.size(); i++) out[i] = nq_record{(uint32_t)g[i].ld, (uint32_t)g[i].rd, (uint32_t)g[i].col, g[i].startijkl};
+    std::vector<GenRecord>().swap(g);
     return NQ_OK;
   };
   cudaStream_t st = h->stream;

@@ -87,6 +87,7 @@ class ServerStats:
     makespan_s: float = 0.0
     batches: int = 0
     max_inflight_seen: int = 0
+    max_admitted_bytes: int = 0     # largest sum of the sized requests in flight at once
 
     def percentile(self, q: float) -> float:
         return float(np.percentile(self.latencies_s, q)) if self.latencies_s else 0.0
@@ -128,6 +129,7 @@ class Server:
         self._done: List[_Request] = []
         self._batches = 0
         self._max_inflight_seen = 0
+        self._max_admitted = 0
         self._t0: Optional[float] = None
         self._t_last = 0.0
         self._error: Optional[BaseException] = None
@@ -173,7 +175,8 @@ class Server:
             span = (self._t_last - self._t0) if self._t0 is not None else 0.0
             return ServerStats(completed=len(self._done), latencies_s=lat, latencies_by_request=by_req,
                                phases_by_request=phases, h2d_bytes=self._h2d, d2h_bytes=8 * len(self._done),
-                               makespan_s=span, batches=self._batches, max_inflight_seen=self._max_inflight_seen)
+                               makespan_s=span, batches=self._batches, max_inflight_seen=self._max_inflight_seen,
+                               max_admitted_bytes=self._max_admitted)
 
     def close(self) -> None:
         with self._cv:
@@ -247,7 +250,8 @@ class Server:
                 self._building -= 1
                 self._cv.notify_all()
             return True
-        nbytes = batch.device_bytes
+        # the sized estimate is an upper bound of the batch's bytes; count whichever is larger against the budget
+        nbytes = max(est, int(batch.device_bytes))
         h2d = getattr(batch, "h2d_bytes", 0)
         if self.share_gpu:
             # small batches take the whole GPU while no large batch runs (they end in
@@ -265,6 +269,7 @@ class Server:
             self._h2d += h2d
             self._building -= 1
             self._admitted += nbytes
+            self._max_admitted = max(self._max_admitted, self._admitted)
             self._batches += 1
             self._max_inflight_seen = max(self._max_inflight_seen, len(self._inflight))
         return True

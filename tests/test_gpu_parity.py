@@ -103,18 +103,18 @@ def test_headline_config_every_record(eng, oracle_mod):
 
 
 def test_large_counts_per_record_low_preset(eng, oracle_mod):
-    """N=22 at preset 4: few records with large counts each (the per-lane counters are sized from a bound
-    on the count per queue item), unsplit and split, per record against the oracle."""
+    """N=21 at preset 4: a few records with large counts each, so the launch takes the u64 per-lane counters
+    (sized from a bound on the count per queue item), split one and two levels, per record against the oracle."""
     import nqueens
-    recs = nqueens.gen_records(22, 4)
-    idx = np.sort(np.random.default_rng(22).choice(len(recs), size=6, replace=False))
+    recs = nqueens.gen_records(21, 4)
+    idx = np.sort(np.random.default_rng(21).choice(len(recs), size=4, replace=False))
     sub = np.ascontiguousarray(recs[idx])
-    want = oracle_mod.exec_solutions(22, _o_records(oracle_mod, sub), threads=0)
+    want = oracle_mod.exec_solutions(21, _o_records(oracle_mod, sub), threads=0)
     old = eng.get_config()
     try:
-        for split in (0, 2):
+        for split in (1, 2):
             eng.set_config(64, 0, split)
-            total, sol = eng.exec_records(22, sub, want_solutions=True)
+            total, sol = eng.exec_records(21, sub, want_solutions=True)
             assert np.array_equal(sol, want), split
     finally:
         eng.set_config(*old)
