@@ -35,8 +35,9 @@
 // TERM is not stored: it is the task's terminal depth T (info word); TALL
 // never occurs in constellation tasks.  compact_fits() checks the fields do
 // not overlap (la < 2^s, RA << s within bits N-1..N).
-// Wide word (8 B, mixed batches and completion queries):
-//   x: bits 0-23 LA | 24-26 s | 27 FC | 28 TERM | 30 TALL;  y: RA
+// Wide word (8 B, mixed batches and completion queries), the same funnel-shift
+// layout for nld with RA in a word of its own (any bits):
+//   x: bits 0-4 s | 5 FC | 6 TERM | 7 TALL | top s bits LA (la < 2^s);  y: RA
 #pragma once
 #include <stdint.h>
 
@@ -56,11 +57,10 @@ constexpr uint32_t C_S = 0x1Fu;
 constexpr uint32_t C_FC = 1u << 28;
 NQ_HD uint32_t compact_ra_mask(int N) { return 3u << (N - 1); }   // where RA << s may sit
 // wide word fields (x)
-constexpr uint32_t W_LA = 0x00FFFFFFu;
-constexpr int W_SSHIFT = 24;
-constexpr uint32_t W_FC = 1u << 27;
-constexpr uint32_t W_TERM = 1u << 28;
-constexpr uint32_t W_TALL = 1u << 30;
+constexpr uint32_t W_S = 0x1Fu;
+constexpr uint32_t W_FC = 1u << 5;
+constexpr uint32_t W_TERM = 1u << 6;
+constexpr uint32_t W_TALL = 1u << 7;
 
 // Known whole-board totals (the reference's known-answer table,
 // 356Py_savesp_narrow.py:5775), index N.  Used only as an upper bound when
@@ -309,9 +309,11 @@ NQ_HD Op unpack_compact(uint32_t w, int N, bool term) {
   o.tall = 0;
   return o;
 }
+// True when the op packs into a wide word: LA in the top s bits clear of the flags (s <= 24).
+NQ_HD bool wide_fits(const Op& o) { return o.s <= 24 && (uint64_t)o.la < (1ull << o.s); }
 NQ_HD uint32_t pack_wide_x(const Op& o) {
-  return (o.la & W_LA) | (o.s << W_SSHIFT) | (o.fc ? W_FC : 0u) | (o.term ? W_TERM : 0u) |
-         (o.tall ? W_TALL : 0u);
+  return o.s | (o.fc ? W_FC : 0u) | (o.term ? W_TERM : 0u) | (o.tall ? W_TALL : 0u) |
+         (o.s ? (o.la << (32 - o.s)) : 0u);
 }
 
 }  // namespace nq

@@ -274,7 +274,7 @@ int build_completion_tasks(int N, int k, const int* rows, const int* cols, int m
   const int T = n - 1;
   extend_lookahead(ops, T);
   for (int d = 0; d < n; d++)
-    if (ops[d].s > 7 || (ops[d].la & ~W_LA)) return -1;
+    if (!wide_fits(ops[d])) return -1;
 
   // Expand the first levels breadth-first until there are enough tasks.
   struct F4 { uint32_t ld, rd, col, avail; };

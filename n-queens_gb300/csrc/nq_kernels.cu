@@ -86,7 +86,7 @@ __device__ __forceinline__ int prepare_one(int N, const uint4* __restrict__ rec,
     typename WordT<WIDE>::type* s = sched + t * sw;
     bool fits = true;
     for (int d = 0; d <= T; d++) {
-      if constexpr (WIDE) s[d] = make_uint2(pack_wide_x(ops[d]), ops[d].ra);
+      if constexpr (WIDE) { fits = fits && wide_fits(ops[d]); s[d] = make_uint2(pack_wide_x(ops[d]), ops[d].ra); }
       else { fits = fits && compact_fits(ops[d], N); s[d] = pack_compact(ops[d]); }
     }
     if (!fits) {                      // never seen (N=6..21, presets 4-7): fail loudly rather than miscount
@@ -137,7 +137,8 @@ __device__ __forceinline__ Dec decode(uint32_t w, uint32_t N, uint32_t k, uint32
   return Dec{o.s, o.la, o.ra, o.fc, o.term, o.tall};
 }
 __device__ __forceinline__ Dec decode(uint2 w, uint32_t, uint32_t, uint32_t) {
-  return Dec{(w.x >> W_SSHIFT) & 7u, w.x & W_LA, w.y, w.x & W_FC, w.x & W_TERM, w.x & W_TALL};
+  const uint32_t s = w.x & W_S;
+  return Dec{s, s ? (w.x >> (32 - s)) : 0u, w.y, w.x & W_FC, w.x & W_TERM, w.x & W_TALL};
 }
 
 // ---------------------------------------------------------------------------
@@ -429,10 +430,12 @@ struct Lane {
     uint32_t nld, nrd;
     bool term, fc, tall = false;
     if constexpr (WIDE) {
-      const Dec o = decode(w, 0u, 0u, 0u);
-      nld = ((ld + bit) << o.s) | o.la;
-      nrd = ((rd + bit) >> o.s) | o.ra;
-      term = o.term != 0u; fc = o.fc != 0u; tall = o.tall != 0u;
+      // the same funnel shift for nld; RA, which may sit anywhere, is or-ed after the right shift
+      asm("shf.l.wrap.b32 %0, %1, %2, %1;" : "=r"(nld) : "r"(w.x), "r"(ld + bit));
+      uint32_t y;
+      asm("shf.r.wrap.b32 %0, %1, 0, %2;" : "=r"(y) : "r"(rd + bit), "r"(w.x));
+      nrd = y | w.y;
+      term = (w.x & W_TERM) != 0u; fc = (w.x & W_FC) != 0u; tall = (w.x & W_TALL) != 0u;
     } else {
       // nld = (x << s) | LA in one funnel shift of the word (LA in its top s bits, s in its low 5);
       // nrd = ((y | RA << s) >> s) = (y >> s) | RA, RA << s or-ed in from the word's bits N-1..N

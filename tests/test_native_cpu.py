@@ -113,8 +113,8 @@ def replay(root, info, words, wide):
         nodes += 1
         if wide:
             x, ra = words[d]
-            s = (x >> 24) & 7; la = x & 0xFFFFFF
-            fc, term, tall = x & (1 << 27), x & (1 << 28), x & (1 << 30)
+            s = x & 31; la = (x >> (32 - s)) if s else 0
+            fc, term, tall = x & (1 << 5), x & (1 << 6), x & (1 << 7)
         else:                        # compact word: s in bits 0-4, RA << s at bits N-1..N, FC bit 28, LA on top
             w = words[d]
             s = w & 31; la = w >> (32 - s); ra = (w & (3 << (N - 1))) >> s
@@ -199,8 +199,8 @@ def test_completion_lookahead_flags(nq):
                 continue
             for d in range(T):
                 x1 = w[d + 1][0]
-                sound = ((x1 >> 24) & 7) == 1 and not (x1 & (1 << 30))
-                assert bool(w[d][0] & (1 << 27)) == sound, (queens, d)
+                sound = (x1 & 31) == 1 and not (x1 & (1 << 7))
+                assert bool(w[d][0] & (1 << 5)) == sound, (queens, d)
 
 
 @pytest.mark.parametrize("N,preset", [(n, p) for n in (8, 11, 14, 17) for p in (4, 5, 6, 7)])
@@ -337,3 +337,20 @@ def test_entry_points_reject_a_null_handle(nq):
     t = np.zeros(1, np.uint64)
     assert L.nq_count(None, 10, 0, _lib.p64(t)) == _lib.NQ_EINVAL
     assert L.nq_set_config(None, 64, 0, -1) == _lib.NQ_EINVAL
+
+
+@pytest.mark.parametrize("N", [8, 16, 20])
+def test_presets_below_four_are_rejected(nq, N):
+    """The start constellations already hold three or four queens, and the reference's presets are 4..8:
+    a preset below 4 is rejected at once with NQ_EPRESET (it used to run the expansion for seconds at N=16
+    and past a minute at N=18), by the generator and by the whole-board sizing call."""
+    import time
+    from nqueens import NQError
+    for preset in (1, 2, 3):
+        t0 = time.perf_counter()
+        with pytest.raises(NQError) as e:
+            nq.gen_records(N, preset)
+        assert e.value.status == -6 and time.perf_counter() - t0 < 1.0
+    with pytest.raises(NQError) as e:
+        nq.engine.job_device_bytes(nq.CountJob(N, 3), 152)
+    assert e.value.status == -6
