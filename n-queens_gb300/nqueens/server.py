@@ -11,7 +11,10 @@ large one.  A scheduler thread admits a lane's queued requests as a new
 batch whenever that lane has a free slot and the device-memory budget allows:
 the batch's tasks are built and uploaded (``nq_batch_create``), then launched
 asynchronously on the batch's own CUDA stream (``nq_batch_submit``), so
-batches admitted while others run overlap them on the GPU.  Finished batches
+batches admitted while others run overlap them on the GPU.  Each request is
+sized when it is submitted (``nq_job_device_bytes``, host-side, no allocation),
+so the budget is a hard limit: a request larger than the whole budget fails
+at once with NQ_ENOMEM, and the bytes in flight never exceed it.  Finished batches
 are polled (bounded waits), their per-job totals resolve the requests'
 futures, and their device memory returns to the budget.
 
@@ -43,6 +46,7 @@ class _Request:
     t_admit: float = 0.0    # taken off the queue into a batch
     t_built: float = 0.0    # its batch built and launched
     t_done: float = 0.0
+    bytes: int = 0          # device bytes of the request, sized when it was submitted
 
 
 @dataclass
@@ -143,12 +147,23 @@ class Server:
             raise TypeError("submit a CountJob or a CompletionJob")
         f: Future = Future()
         now = time.perf_counter()
+        # Size the request here, on the caller's thread and outside the server's lock: the first sizing of a
+        # large board generates its constellations (about a second at N=22), which must not stall the scheduler.
+        try:
+            nbytes = self._job_bytes(job)
+        except NQError as exc:
+            f.set_exception(exc)
+            return f
+        if nbytes > self.budget:               # can never fit: fails alone, nothing is queued
+            f.set_exception(NQError(-5, f"request needs about {nbytes} device bytes, more than the server's "
+                                        f"budget of {self.budget}"))
+            return f
         with self._cv:
             if self._error is not None:
                 raise RuntimeError("server stopped after an error") from self._error
             if self._t0 is None:
                 self._t0 = now
-            r = _Request(job, f, now, self._seq)
+            r = _Request(job, f, now, self._seq, bytes=nbytes)
             self._seq += 1
             (self._pending_large if estimate_ms(job, self._count_ms) > self.large_ms else self._pending).append(r)
             self._cv.notify()
@@ -226,12 +241,7 @@ class Server:
             take: List[_Request] = []
             est = 0
             while queue and len(take) < (1 if large else self.max_batch_jobs):
-                e = self._job_bytes(queue[0].job)
-                if e > self.budget:        # can never fit: fails alone, the queue moves on
-                    r = queue.popleft()
-                    r.future.set_exception(NQError(-5, f"request needs about {e} device bytes, more than the "
-                                                       f"server's budget of {self.budget}"))
-                    continue
+                e = queue[0].bytes
                 if take and self._admitted + est + e > self.budget:
                     break
                 if not take and self._admitted + e > self.budget:
