@@ -97,6 +97,10 @@ int nq_exec_solutions(nq_handle *h, int N, const nq_record *records, int64_t m, 
  * status. */
 int nq_exec_solutions_device(nq_handle *h, int N, const nq_record *d_records, int64_t m, int start_min,
                              uint64_t *d_solutions, uint64_t *d_total, void *stream);
+/* Waits for the handle's last nq_exec_solutions_device call (an event
+ * recorded on its stream; other handles, batches and streams are not waited
+ * for) and returns its device status; with nothing outstanding, waits for the
+ * handle's own stream. */
 int nq_sync(nq_handle *h);
 /* Device time of the last exec_solutions call's prepare and DFS kernels
  * (CUDA events recorded on the launching stream); waits for them. */
@@ -154,7 +158,9 @@ int nq_last_count_info(const nq_handle *h, int64_t *chunks, int64_t *records);
 
 /* Unique (distinct under rotation and reflection) and total counts by the
  * symmetry method (11Bit_Python/07Py_bit_symmetry.py:65-200; GPU form
- * 10Bit_CUDA/01CUDA_Bit_Symmetry.cu:627-960).  4 <= N <= 27. */
+ * 10Bit_CUDA/01CUDA_Bit_Symmetry.cu:627-960).  4 <= N <= 27.  Runs on the
+ * handle's device and stream with buffers the handle keeps between calls;
+ * failures are reported through nq_last_error like every other call. */
 int nq_count_unique(nq_handle *h, int N, uint64_t *unique, uint64_t *total);
 
 /* Completions of a board with k pre-placed queens (rows[i], cols[i]; column c
