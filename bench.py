@@ -352,7 +352,7 @@ def ours_arm(args):
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u32", "data": "synthetic",
         "config": bench_config(N),
-        "launch": {"per_step": "one prepare + split + DFS launch sequence", "block": args.block,
+        "launch": {"per_step": "one prepare + split + DFS launch sequence", "block": eng.get_config()[0],
                    "split_depth": split_depth, "queued_subtasks": queued, "parallelism": f"replicas x{ws}"},
         "total": expected,
         "wall_s": wall_s,
@@ -623,7 +623,8 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--block", type=int, default=64)
+    ap.add_argument("--block", type=int, default=64,
+                    help="threads per block; 64 with --split -1 keeps the autotuned per-N table (nqueens/tuning.json)")
     ap.add_argument("--split", type=int, default=-1, help="split depth (-1 automatic)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")

@@ -112,12 +112,8 @@ struct UArgs {
   unsigned int* err;
 };
 
-// Predicated shared-memory frame load/store (32-bit shared-window addresses),
-// so the pop and the push are single predicated instructions, not branches.
-__device__ __forceinline__ void lds_frame_if(uint32_t p, uint32_t a, uint32_t& x, uint32_t& y, uint32_t& z, uint32_t& w) {
-  asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %4, 0;\n\t@q ld.shared.v4.u32 {%0, %1, %2, %3}, [%5];\n\t}"
-               : "+r"(x), "+r"(y), "+r"(z), "+r"(w) : "r"(p), "r"(a));
-}
+// Predicated shared-memory stores (32-bit shared-window addresses), so the push is
+// a single predicated instruction, not a branch.
 __device__ __forceinline__ void sts_frame_if(uint32_t p, uint32_t a, uint32_t x, uint32_t y, uint32_t z, uint32_t w) {
   asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %0, 0;\n\t@q st.shared.v4.u32 [%1], {%2, %3, %4, %5};\n\t}"
                :: "r"(p), "r"(a), "r"(x), "r"(y), "r"(z), "r"(w) : "memory");
@@ -183,9 +179,10 @@ __global__ void __launch_bounds__(BLOCK) unique_kernel(const UArgs a) {
     // kUniqueSteps steps between two checks for finished lanes (two ballots each)
 #pragma unroll 1
     for (int s = 0; s < kUniqueSteps; ++s) {
-      const uint32_t pop = (avail == 0u && sp != sbase) ? 1u : 0u;
-      sp -= pop ? F : 0u;
-      lds_frame_if(pop, sp, left, down, right, avail);
+      // pop with its condition formed in a predicate register inside the block (no 0/1 value for it)
+      asm volatile("{\n\t.reg .pred q;\n\tsetp.eq.u32 q, %3, 0;\n\tsetp.ne.and.u32 q, %4, %5, q;\n\t"
+                   "@q sub.u32 %4, %4, %6;\n\t@q ld.shared.v4.u32 {%0, %1, %2, %3}, [%4];\n\t}"
+                   : "+r"(left), "+r"(down), "+r"(right), "+r"(avail), "+r"(sp) : "r"(sbase), "n"(F));
       const uint32_t row = __umulhi(down, 32u);                 // down >> 27
       const bool act = avail != 0u;
       const uint32_t bit = avail & (0u - avail);

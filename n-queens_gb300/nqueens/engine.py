@@ -310,6 +310,7 @@ class Engine:
     def exec_device(self, N: int, d_records: int, m: int, start_min: int, d_total: int,
                     d_solutions: int = 0, stream: int = 0) -> None:
         """Asynchronous count of device-resident records (raw device pointers); see sync()."""
+        self._apply_tuning(N)
         _check(lib().nq_exec_solutions_device(self._h, int(N), ctypes.c_void_p(d_records), int(m), int(start_min),
                                               ctypes.c_void_p(d_solutions or None), ctypes.c_void_p(d_total),
                                               ctypes.c_void_p(stream or None)), self._h, f"exec_device(N={N})")
