@@ -150,6 +150,21 @@ int nq_tune(nq_handle *h, int N, int repeats, int *best_block, int *best_split, 
  * at the largest boards: the next chunk is generated while the previous one
  * counts on the GPU. */
 int nq_count(nq_handle *h, int N, int preset, uint64_t *total);
+/* The canonical start constellations of N (6 <= N <= 27; packed
+ * i<<15 | j<<10 | k<<5 | l, ascending), the first stage of
+ * gen_constellations (356Py_savesp_narrow.py:2837-2880).  Writes them when
+ * out != NULL and cap is large enough; returns their number or a negative
+ * status.  Host only. */
+int64_t nq_start_constellations(int N, int32_t *out, int64_t cap);
+/* The part of nq_count(N, preset) that comes from start constellations
+ * [first, first + count) of nq_start_constellations' list: the records those
+ * starts expand into (preset <= 0: nq_preset_for(N)), streamed the same way.
+ * Totals over a partition of the list add up to the whole-board total, so a
+ * long count can be cut at start boundaries and resumed -- the reference's
+ * restart unit is the chunk of its task list (chunk_only / debug_chunk_start,
+ * 356Py_savesp_narrow.py:2418-2435, with a progress TSV, :3330-3338).  A range
+ * outside the list is NQ_EINVAL; an empty range counts 0. */
+int nq_count_starts(nq_handle *h, int N, int preset, int64_t first, int64_t count, uint64_t *total);
 /* Records per chunk of nq_count (0: the default, 8 Mi records, about 32 MB of
  * host records per chunk; one chunk up to N=21). */
 int nq_set_chunk_records(nq_handle *h, int64_t records);

@@ -491,22 +491,20 @@ int nq_set_chunk_records(nq_handle* h, int64_t records) {
   return NQ_OK;
 }
 
-// Whole-board count, generated and counted chunk by chunk so host memory stays
-// bounded for the largest boards (the reference streams its task list to a
-// .bin file for the same reason, gen_constellations_stream_to_bin,
-// 356Py_savesp_narrow.py:2988-3084): the start constellations are listed
-// first (cheap), then each chunk of them is expanded into records on the host
-// threads while the previous chunk's DFS runs on the GPU.
-int nq_count(nq_handle* h, int N, int preset, uint64_t* total) {
-  if (!h || !total) return NQ_EINVAL;
-  if (N < 1 || N > kMaxN) return h->fail(NQ_EINVAL, "N=%d outside 1..27", N);
-  if (N <= 5) return nq_count_completions(h, N, 0, nullptr, nullptr, total);
-  const int p = preset > 0 ? preset : preset_for(N);
-  if (p < 4) return h->fail(NQ_EPRESET, "generator: preset %d below 4", p);
-  std::vector<int> starts;
-  if (start_constellations(N, starts) != 0) return h->fail(NQ_EINVAL, "generator: bad arguments N=%d", N);
+}  // extern "C"
+
+namespace {
+
+// The records of start constellations [s_begin, s_end), generated and counted
+// chunk by chunk so host memory stays bounded for the largest boards (the
+// reference streams its task list to a .bin file for the same reason,
+// gen_constellations_stream_to_bin, 356Py_savesp_narrow.py:2988-3084): each
+// chunk of starts is expanded into records on the host threads while the
+// previous chunk's DFS runs on the GPU.
+int count_start_range(nq_handle* h, int N, int p, const std::vector<int>& starts, size_t s_begin, size_t s_end,
+                      uint64_t* total) {
   const int64_t chunk = h->chunk_records > 0 ? h->chunk_records : kChunkRecords;
-  size_t next = 0;
+  size_t next = s_begin;
   double per_start = 0.0;                  // records per start constellation seen so far
   std::vector<GenRecord> g;
   // Blocks of starts are expanded and packed into 16-byte records at once, so the
@@ -514,11 +512,11 @@ int nq_count(nq_handle* h, int N, int preset, uint64_t* total) {
   auto gen_chunk = [&](std::vector<nq_record>& out) -> int {
     out.clear();
     if (per_start > 0.0)   // expected size of this chunk, so the vector does not double past it
-      out.reserve((size_t)std::min((double)(chunk + chunk / 8), per_start * (double)(starts.size() - next) + 1024.0));
-    while (next < starts.size() && (int64_t)out.size() < chunk) {
+      out.reserve((size_t)std::min((double)(chunk + chunk / 8), per_start * (double)(s_end - next) + 1024.0));
+    while (next < s_end && (int64_t)out.size() < chunk) {
       const double want = std::min((double)(chunk - (int64_t)out.size()), (double)chunk / 8.0);
       const size_t take = per_start > 0.0 ? (size_t)std::max(1.0, want / per_start) : (size_t)16;
-      const size_t s1 = std::min(starts.size(), next + take);
+      const size_t s1 = std::min(s_end, next + take);
       g.clear();
       const int e = expand_starts(N, p, starts, next, s1, g, 0);
       if (e == -1) return h->fail(NQ_EINVAL, "generator: bad arguments N=%d preset=%d", N, p);
@@ -556,6 +554,47 @@ int nq_count(nq_handle* h, int N, int preset, uint64_t* total) {
   h->last_records = records;
   *total = acc;
   return NQ_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Whole-board count: the start constellations are listed first (cheap), then
+// counted as one range.
+int nq_count(nq_handle* h, int N, int preset, uint64_t* total) {
+  if (!h || !total) return NQ_EINVAL;
+  if (N < 1 || N > kMaxN) return h->fail(NQ_EINVAL, "N=%d outside 1..27", N);
+  if (N <= 5) return nq_count_completions(h, N, 0, nullptr, nullptr, total);
+  const int p = preset > 0 ? preset : preset_for(N);
+  if (p < 4) return h->fail(NQ_EPRESET, "generator: preset %d below 4", p);
+  std::vector<int> starts;
+  if (start_constellations(N, starts) != 0) return h->fail(NQ_EINVAL, "generator: bad arguments N=%d", N);
+  return count_start_range(h, N, p, starts, 0, starts.size(), total);
+}
+
+int64_t nq_start_constellations(int N, int32_t* out, int64_t cap) {
+  if (N < 6 || N > kMaxN) return NQ_EINVAL;
+  std::vector<int> starts;
+  if (start_constellations(N, starts) != 0) return NQ_EINVAL;
+  const int64_t n = (int64_t)starts.size();
+  if (out && cap >= n)
+    for (int64_t i = 0; i < n; i++) out[i] = (int32_t)starts[i];
+  return n;
+}
+
+int nq_count_starts(nq_handle* h, int N, int preset, int64_t first, int64_t count, uint64_t* total) {
+  if (!h || !total) return NQ_EINVAL;
+  if (N < 6 || N > kMaxN) return h->fail(NQ_EINVAL, "count_starts: N=%d outside 6..27", N);
+  const int p = preset > 0 ? preset : preset_for(N);
+  if (p < 4) return h->fail(NQ_EPRESET, "generator: preset %d below 4", p);
+  std::vector<int> starts;
+  if (start_constellations(N, starts) != 0) return h->fail(NQ_EINVAL, "generator: bad arguments N=%d", N);
+  const int64_t ns = (int64_t)starts.size();
+  if (first < 0 || count < 0 || first > ns || count > ns - first)
+    return h->fail(NQ_EINVAL, "count_starts: range [%lld, +%lld) outside the %lld start constellations",
+                   (long long)first, (long long)count, (long long)ns);
+  return count_start_range(h, N, p, starts, (size_t)first, (size_t)(first + count), total);
 }
 
 int nq_last_count_info(const nq_handle* h, int64_t* chunks, int64_t* records) {

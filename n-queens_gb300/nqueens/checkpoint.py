@@ -7,6 +7,12 @@ cut into fixed chunks; after each chunk one line ``chunk<TAB>first<TAB>end<TAB>t
 is appended to the progress file and flushed, and a rerun skips the chunks
 already recorded.  The file starts with a header naming N, the record count and
 a digest of the records, so a progress file never resumes a different task list.
+
+``count_resumable`` does the same for a whole-board count without holding the
+task list: its chunks are ranges of the board's start constellations, each
+generated and counted on the GPU by ``Engine.count_starts`` (host memory stays
+bounded), so a count longer than one sitting -- N=24 and up -- is spread over
+several runs that share the progress file.
 """
 from __future__ import annotations
 
@@ -17,6 +23,7 @@ from typing import Callable, Dict, Optional
 import numpy as np
 
 from ._lib import RECORD_DTYPE
+from .engine import select_dynamic_preset_queens, start_constellations
 
 
 def _digest(records: np.ndarray) -> str:
@@ -71,4 +78,41 @@ def exec_records_resumable(counter: Callable[[int, np.ndarray], int], N: int, re
             os.fsync(f.fileno())
             done[c] = t
             counted += 1
+    return sum(done[c] for c in range(n_chunks))
+
+
+def _starts_header(N: int, preset: int, starts: np.ndarray, chunk: int) -> str:
+    d = hashlib.sha256(np.ascontiguousarray(starts, np.int32).tobytes()).hexdigest()[:32]
+    return f"# nqueens progress N={N} preset={preset} starts={len(starts)} chunk={chunk} sha256={d}\n"
+
+
+def count_resumable(eng, N: int, progress_path: str, preset: Optional[int] = None, chunk: int = 64,
+                    stop_after: Optional[int] = None, log: Optional[Callable[[str], None]] = None) -> Optional[int]:
+    """Whole-board total of N, counted in chunks of ``chunk`` start constellations with
+    ``eng.count_starts`` and resumed from progress_path.  ``stop_after`` returns None after that
+    many newly counted chunks (an interruption, for tests, or a run cut to fit a time limit)."""
+    p = select_dynamic_preset_queens(N) if preset is None else int(preset)
+    starts = start_constellations(N)
+    header = _starts_header(N, p, starts, chunk)
+    done = read_progress(progress_path, header)
+    if not os.path.exists(progress_path):
+        with open(progress_path, "w") as f:
+            f.write(header)
+    n_chunks = (len(starts) + chunk - 1) // chunk
+    counted = 0
+    with open(progress_path, "a") as f:
+        for c in range(n_chunks):
+            if c in done:
+                continue
+            if stop_after is not None and counted >= stop_after:
+                return None
+            a, b = c * chunk, min(len(starts), (c + 1) * chunk)
+            t = eng.count_starts(N, a, b - a, p)
+            f.write(f"{c}\t{a}\t{b}\t{t}\n")
+            f.flush()
+            os.fsync(f.fileno())
+            done[c] = t
+            counted += 1
+            if log:
+                log(f"N={N} chunk {c + 1}/{n_chunks} starts [{a}, {b}) total {t}")
     return sum(done[c] for c in range(n_chunks))

@@ -14,6 +14,11 @@ the constellation path, as in the reference, unless --unique is given.
 --repeat runs each count R times (the last one is printed), which is how
 profiles/ captures a warm kernel.
 
+--progress FILE counts one board (nmin, with nmax = nmin + 1) in chunks of
+start constellations, appending each chunk's total to FILE and skipping the
+chunks already there, so a count too long for one run is finished by rerunning
+the same command (--stop-after C ends a run after C new chunks).
+
 --tasks counts one of the reference's cached task files (16-byte records,
 N taken from the file name or --n) and --write-solutions writes the
 per-record counts as the reference's 40-byte solutions_*_v2.bin cache.  The
@@ -88,6 +93,28 @@ def _count_regenerated(a) -> int:
     return _count_records(a, N, gen_records(N, preset), gen_records_wide(N, preset), f"N={N} generated")
 
 
+def _count_with_progress(a) -> int:
+    from .checkpoint import count_resumable
+    N = a.nmin
+    if a.nmax != N + 1 or not 6 <= N <= 27:
+        print("--progress counts one board: give nmin and nmax = nmin + 1, 6 <= nmin <= 27", file=sys.stderr)
+        return 2
+    eng = Engine(a.device, block=a.block, split=a.split)
+    try:
+        t0 = dt.datetime.now()
+        total = count_resumable(eng, N, a.progress, a.preset or None, a.chunk_starts, a.stop_after,
+                                log=lambda m: print(m, file=sys.stderr, flush=True))
+        el = dt.datetime.now() - t0
+    finally:
+        eng.close()
+    if total is None:
+        print(f"{N:2d}: stopped after {a.stop_after} chunks ({_fmt(el)}); rerun to continue from {a.progress}")
+        return 0
+    status = "ok" if N < len(EXPECTED) and EXPECTED[N] == total else f"ng({total}!={EXPECTED[N]})"
+    print(f"{N:2d}:{total:18d}{0:17d}{_fmt(el):>21s}    {status}")
+    return 0 if status == "ok" else 1
+
+
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser(prog="python -m nqueens", description=__doc__.split("\n")[0])
     ap.add_argument("nmin", nargs="?", type=int, default=5)
@@ -103,8 +130,14 @@ def main(argv=None) -> int:
                                               "solutions file")
     ap.add_argument("--regenerate", action="store_true",
                     help="with --n: generate the constellations (full-width masks) instead of reading --tasks")
-    ap.add_argument("--preset", type=int, default=0, help="with --regenerate: preset queens (0: the dynamic preset)")
+    ap.add_argument("--preset", type=int, default=0,
+                    help="with --regenerate or --progress: preset queens (0: the dynamic preset)")
+    ap.add_argument("--progress", help="count board nmin resumably, keeping per-chunk totals in this file")
+    ap.add_argument("--chunk-starts", type=int, default=64, help="with --progress: start constellations per chunk")
+    ap.add_argument("--stop-after", type=int, default=None, help="with --progress: stop after this many new chunks")
     a = ap.parse_args(argv)
+    if a.progress:
+        return _count_with_progress(a)
     if a.regenerate:
         return _count_regenerated(a)
     if a.tasks:

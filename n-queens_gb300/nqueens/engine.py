@@ -65,6 +65,19 @@ def gen_records(N: int, preset: Optional[int] = None) -> np.ndarray:
     return out
 
 
+def start_constellations(N: int) -> np.ndarray:
+    """The canonical start constellations of N (packed i<<15|j<<10|k<<5|l, ascending, int32): the
+    units nq_count_starts counts, the first stage of gen_constellations (356Py:2837-2880)."""
+    L = lib()
+    n = L.nq_start_constellations(int(N), None, 0)
+    if n < 0:
+        _check(int(n), what=f"start_constellations(N={N})")
+    out = np.zeros(n, np.int32)
+    if L.nq_start_constellations(int(N), out.ctypes.data_as(ctypes.c_void_p), n) != n:
+        raise NQError(_lib.NQ_EINVAL, "start list changed between calls")
+    return out
+
+
 def gen_records_wide(N: int, preset: Optional[int] = None) -> Tuple[np.ndarray, np.ndarray, np.ndarray, np.ndarray]:
     """(ld, rd, col, startijkl) with the reference's full-width masks (uint64, uint64, uint64, uint32)."""
     p = select_dynamic_preset_queens(N) if preset is None else int(preset)
@@ -342,6 +355,15 @@ class Engine:
         self._apply_tuning(N)
         _check(lib().nq_count(self._h, int(N), int(preset or 0), _lib.p64(t)), self._h, f"count(N={N})")
         return Result(total=int(t[0]))
+
+    def count_starts(self, N: int, first: int, count: int, preset: Optional[int] = None) -> int:
+        """The part of count(N, preset) that comes from start constellations [first, first+count)
+        of start_constellations(N); totals over a partition of the list add up to count(N)."""
+        t = np.zeros(1, np.uint64)
+        self._apply_tuning(N)
+        _check(lib().nq_count_starts(self._h, int(N), int(preset or 0), int(first), int(count), _lib.p64(t)),
+               self._h, f"count_starts(N={N}, {first}, {count})")
+        return int(t[0])
 
     def set_chunk_records(self, records: int) -> None:
         """Records per chunk of count() (0: the library default); bounds the host memory of large boards."""

@@ -377,3 +377,56 @@ def test_queue_order_leaves_counts_unchanged(eng, oracle_mod):
     finally:
         eng.set_queue_order(0)
         eng.set_config(*old)
+
+
+def test_count_starts_ranges_match_oracle(eng, oracle_mod):
+    """count_starts(first, count) counts exactly the records whose start constellation lies in that range
+    of start_constellations(N): each range against the oracle's per-record counts of those records, and
+    an uneven partition adds up to the whole board."""
+    import nqueens
+    N = 14
+    starts = nqueens.start_constellations(N)
+    recs = nqueens.gen_records(N)
+    per = oracle_mod.exec_solutions(N, _o_records(oracle_mod, recs))
+    key = (recs["startijkl"] & 0xFFFFF).astype(np.int32)
+    cuts = [0, 1, 7, 300, 301, 1000, len(starts)]
+    acc = 0
+    for a, b in zip(cuts[:-1], cuts[1:]):
+        t = eng.count_starts(N, a, b - a)
+        assert t == int(per[np.isin(key, starts[a:b])].sum()), (a, b)
+        acc += t
+    assert acc == oracle_mod.EXPECTED_TOTAL[N]
+    assert eng.count_starts(N, 5, 0) == 0
+    assert eng.count_starts(N, len(starts), 0) == 0
+    for a, c in [(-1, 1), (0, len(starts) + 1), (len(starts), 1)]:
+        with pytest.raises(nqueens.NQError) as ei:
+            eng.count_starts(N, a, c)
+        assert "start constellations" in str(ei.value)
+
+
+@pytest.mark.parametrize("N,chunk", [(16, 500), (19, 4000)])
+def test_count_resumable_by_start_ranges(oracle_mod, tmp_path, N, chunk):
+    """A whole-board count cut at start-constellation boundaries, interrupted and resumed from its progress
+    file, gives the known total and counts no range twice."""
+    import nqueens
+    from nqueens.checkpoint import count_resumable
+    e = nqueens.Engine(0)
+    p = str(tmp_path / "progress.tsv")
+    try:
+        assert count_resumable(e, N, p, chunk=chunk, stop_after=1) is None
+        assert count_resumable(e, N, p, chunk=chunk) == oracle_mod.EXPECTED_TOTAL[N]
+        lines = open(p).read().splitlines()[1:]
+        n_starts = len(nqueens.start_constellations(N))
+        assert len(lines) == (n_starts + chunk - 1) // chunk
+        assert sorted(int(x.split("\t")[0]) for x in lines) == list(range(len(lines)))
+    finally:
+        e.close()
+
+
+def test_cli_progress_resumes(tmp_path, capsys):
+    from nqueens.cli import main
+    p = str(tmp_path / "p.tsv")
+    assert main(["15", "16", "--progress", p, "--chunk-starts", "300", "--stop-after", "2"]) == 0
+    assert "stopped after 2 chunks" in capsys.readouterr().out
+    assert main(["15", "16", "--progress", p, "--chunk-starts", "300"]) == 0
+    assert "2279184" in capsys.readouterr().out
