@@ -18,6 +18,7 @@ from __future__ import annotations
 
 import hashlib
 import os
+import time
 from typing import Callable, Dict, Optional
 
 import numpy as np
@@ -87,10 +88,12 @@ def _starts_header(N: int, preset: int, starts: np.ndarray, chunk: int) -> str:
 
 
 def count_resumable(eng, N: int, progress_path: str, preset: Optional[int] = None, chunk: int = 64,
-                    stop_after: Optional[int] = None, log: Optional[Callable[[str], None]] = None) -> Optional[int]:
+                    stop_after: Optional[int] = None, log: Optional[Callable[[str], None]] = None,
+                    time_limit: Optional[float] = None) -> Optional[int]:
     """Whole-board total of N, counted in chunks of ``chunk`` start constellations with
-    ``eng.count_starts`` and resumed from progress_path.  ``stop_after`` returns None after that
-    many newly counted chunks (an interruption, for tests, or a run cut to fit a time limit)."""
+    ``eng.count_starts`` and resumed from progress_path.  Returns None, leaving the rest for a later
+    run, after ``stop_after`` newly counted chunks, or when ``time_limit`` seconds would be passed:
+    no chunk starts unless 1.5 x the longest chunk of this run still fits."""
     p = select_dynamic_preset_queens(N) if preset is None else int(preset)
     starts = start_constellations(N)
     header = _starts_header(N, p, starts, chunk)
@@ -100,19 +103,25 @@ def count_resumable(eng, N: int, progress_path: str, preset: Optional[int] = Non
             f.write(header)
     n_chunks = (len(starts) + chunk - 1) // chunk
     counted = 0
+    t_start = time.monotonic()
+    longest = 0.0
     with open(progress_path, "a") as f:
         for c in range(n_chunks):
             if c in done:
                 continue
             if stop_after is not None and counted >= stop_after:
                 return None
+            if time_limit is not None and time.monotonic() - t_start + 1.5 * longest > time_limit:
+                return None
             a, b = c * chunk, min(len(starts), (c + 1) * chunk)
+            t0 = time.monotonic()
             t = eng.count_starts(N, a, b - a, p)
+            longest = max(longest, time.monotonic() - t0)
             f.write(f"{c}\t{a}\t{b}\t{t}\n")
             f.flush()
             os.fsync(f.fileno())
             done[c] = t
             counted += 1
             if log:
-                log(f"N={N} chunk {c + 1}/{n_chunks} starts [{a}, {b}) total {t}")
+                log(f"N={N} chunk {c + 1}/{n_chunks} starts [{a}, {b}) total {t} {time.monotonic() - t0:.1f} s")
     return sum(done[c] for c in range(n_chunks))

@@ -17,7 +17,8 @@ profiles/ captures a warm kernel.
 --progress FILE counts one board (nmin, with nmax = nmin + 1) in chunks of
 start constellations, appending each chunk's total to FILE and skipping the
 chunks already there, so a count too long for one run is finished by rerunning
-the same command (--stop-after C ends a run after C new chunks).
+the same command (--stop-after C ends a run after C new chunks, --time-limit S
+before a chunk that would end past S seconds).
 
 --tasks counts one of the reference's cached task files (16-byte records,
 N taken from the file name or --n) and --write-solutions writes the
@@ -103,12 +104,12 @@ def _count_with_progress(a) -> int:
     try:
         t0 = dt.datetime.now()
         total = count_resumable(eng, N, a.progress, a.preset or None, a.chunk_starts, a.stop_after,
-                                log=lambda m: print(m, file=sys.stderr, flush=True))
+                                log=lambda m: print(m, file=sys.stderr, flush=True), time_limit=a.time_limit)
         el = dt.datetime.now() - t0
     finally:
         eng.close()
     if total is None:
-        print(f"{N:2d}: stopped after {a.stop_after} chunks ({_fmt(el)}); rerun to continue from {a.progress}")
+        print(f"{N:2d}: stopped ({_fmt(el)}); rerun to continue from {a.progress}")
         return 0
     status = "ok" if N < len(EXPECTED) and EXPECTED[N] == total else f"ng({total}!={EXPECTED[N]})"
     print(f"{N:2d}:{total:18d}{0:17d}{_fmt(el):>21s}    {status}")
@@ -135,6 +136,8 @@ def main(argv=None) -> int:
     ap.add_argument("--progress", help="count board nmin resumably, keeping per-chunk totals in this file")
     ap.add_argument("--chunk-starts", type=int, default=64, help="with --progress: start constellations per chunk")
     ap.add_argument("--stop-after", type=int, default=None, help="with --progress: stop after this many new chunks")
+    ap.add_argument("--time-limit", type=float, default=None,
+                    help="with --progress: start no chunk that would end past this many seconds")
     a = ap.parse_args(argv)
     if a.progress:
         return _count_with_progress(a)

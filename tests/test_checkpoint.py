@@ -112,3 +112,24 @@ def test_cli_progress_needs_one_board(tmp_path, capsys):
     from nqueens.cli import main
     assert main(["15", "17", "--progress", str(tmp_path / "p.tsv")]) == 2
     assert not (tmp_path / "p.tsv").exists()
+
+
+def test_count_resumable_time_limit(tmp_path, oracle_mod):
+    """With a time limit no chunk starts unless 1.5 x the longest chunk so far still fits; the next run
+    goes on from the progress file."""
+    import time
+    from nqueens.checkpoint import count_resumable
+    N = 12
+    e = _StartsEngine(oracle_mod, N)
+    slow = e.count_starts
+
+    def count_starts(*args):
+        time.sleep(0.2)
+        return slow(*args)
+    e.count_starts = count_starts
+    p = str(tmp_path / "progress.tsv")
+    assert count_resumable(e, N, p, chunk=100, time_limit=0.5) is None
+    assert 1 <= len(e.calls) <= 2
+    e.count_starts = slow
+    assert count_resumable(e, N, p, chunk=100) == oracle_mod.EXPECTED_TOTAL[N]
+    assert len(e.calls) == (len(e.starts) + 99) // 100

