@@ -374,7 +374,6 @@ __device__ __forceinline__ void flush_job(const DfsArgs& a, unsigned job, unsign
 
 // Saved frames per lane: at most one per depth 0..T'-1 above the sentinel.
 __host__ __device__ constexpr int stack_slots(int maxt) { return maxt + 1; }
-constexpr uint32_t SENT_COL = 0x07FFFFFFu;   // sentinel frame's col: every column blocked, depth 0
 
 size_t dfs_smem_bytes(bool wide, int block, int maxt) {
   return (size_t)block * ((size_t)stack_slots(maxt) * sizeof(uint4) + (size_t)(maxt + 1) * (wide ? 8 : 4));
@@ -383,12 +382,11 @@ size_t dfs_smem_bytes(bool wide, int block, int maxt) {
 // One lane's DFS state and its step.  Every lane runs the same predicated
 // sequence each step: resume a saved frame if the current one is exhausted,
 // take the lowest candidate, build the child with the depth's schedule word,
-// apply the look-ahead, then count (terminal depth) or descend.  '+' replaces
-// '|' where the bits are disjoint (a candidate is never in ld, rd or col),
-// so those adds issue on the FMA pipe as well as the ALU pipe.  Per-task
-// counts are u32 (BIG: u64, where a queue item may count 2^32 solutions).
-static_assert(kMaxN <= 27, "a frame's depth is kept in col bits 27-31");
-
+// apply the look-ahead, then count (terminal depth) or descend.  '+' and '-'
+// replace '|' and '&~' where the bits are disjoint (a candidate is never in ld
+// or rd, and always one of the free columns), so those ops issue on the FMA
+// pipe as well as the ALU pipe.  Per-task counts are u32 (BIG: u64, where a
+// queue item may count 2^32 solutions).
 // Shared-memory accesses of the step, as predicated PTX so the pop and the push
 // are single predicated instructions rather than branches around them.
 // Addresses are 32-bit shared-window addresses.
@@ -405,29 +403,33 @@ __device__ __forceinline__ uint2 lds_word(uint32_t a, uint2) {
 
 template <bool WIDE, bool BIG>
 struct Lane {
-  // col bits 27-31 hold the depth of the frame (bm masks them out of every use
-  // of col as a column set), so a saved frame is exactly {ld, rd, col, avail}
-  uint32_t ld = 0, rd = 0, col = 0, avail = 0, bm = 0;
+  // A frame is {ld, rd, fr, avail}: fr holds the columns still free at the frame's
+  // row (one fewer per level, so a frame's depth is popc(root fr) - popc(fr) and
+  // needs no field of its own) and avail the candidates, a subset of fr.
+  uint32_t ld = 0, rd = 0, fr = 0, avail = 0;
   uint32_t sp = 0;      // shared address of the next free frame of this lane's stack
   uint32_t sbase = 0;   // shared address of its first frame: the stack is empty when sp == sbase
-  uint32_t tl = 0;      // terminal depth of the subtask (relative to its root)
+  uint32_t sw0 = 0;     // shared address of the word of the depth where popc(fr) == 0 (word d sits at
+                        // sw0 - popc(fr) * row, row = BLOCK words, since popc(fr) = R - d, R = popc(root fr))
+  uint32_t tf = 0;      // popc(fr) at the subtask's terminal depth: R - terminal depth
   uint32_t ram = 0;     // compact words: the bits where RA << s may sit (compact_ra_mask)
   typename std::conditional<BIG, unsigned long long, uint32_t>::type cnt = 0;
 
   template <int BLOCK>
-  __device__ __forceinline__ void step(uint32_t sch) {
+  __device__ __forceinline__ void step() {
     using W = typename WordT<WIDE>::type;
     constexpr uint32_t F = BLOCK * (uint32_t)sizeof(uint4);
+    constexpr uint32_t ROW = BLOCK * (uint32_t)sizeof(W);
     // pop (the current frame is exhausted and a saved one is left): the condition is formed in a
     // predicate register inside the block, so no 0/1 value is materialised for it (2 % faster at N=19)
     asm volatile("{\n\t.reg .pred p;\n\tsetp.eq.u32 p, %3, 0;\n\tsetp.ne.and.u32 p, %4, %5, p;\n\t"
                  "@p sub.u32 %4, %4, %6;\n\t@p ld.shared.v4.u32 {%0, %1, %2, %3}, [%4];\n\t}"
-                 : "+r"(ld), "+r"(rd), "+r"(col), "+r"(avail), "+r"(sp) : "r"(sbase), "n"(F));
-    const uint32_t d = __umulhi(col, 32u);          // col >> 27, on the FMA pipe
+                 : "+r"(ld), "+r"(rd), "+r"(fr), "+r"(avail), "+r"(sp) : "r"(sbase), "n"(F));
+    const uint32_t pf = __popc(fr);                  // R - depth
     const bool act = avail != 0;
     const uint32_t bit = avail & (0u - avail);
     avail -= bit;
-    const W w = lds_word(sch + d * (BLOCK * (uint32_t)sizeof(W)), W{});
+    const W w = lds_word(sw0 - pf * ROW, W{});
     uint32_t nld, nrd;
     bool term, fc, tall = false;
     if constexpr (WIDE) {
@@ -444,10 +446,9 @@ struct Lane {
       uint32_t y;
       asm("lop3.b32 %0, %1, %2, %3, 0xF8;" : "=r"(y) : "r"(rd + bit), "r"(w), "r"(ram));   // a | (b & c)
       asm("shf.r.wrap.b32 %0, %1, 0, %2;" : "=r"(nrd) : "r"(y), "r"(w));
-      term = d == tl; fc = (w & C_FC) != 0u;
+      term = pf == tf; fc = (w & C_FC) != 0u;
     }
-    const uint32_t ncol = col + bit;
-    const uint32_t free_cols = bm & ~ncol;
+    const uint32_t free_cols = fr - bit;             // the child row's free columns
     const uint32_t nf = free_cols & ~(nld | nrd);
     const uint32_t ahead = free_cols & ~((nld + nld) | __umulhi(nrd, 0x80000000u));   // nrd >> 1
     // terminal depth: count the child (the SQd2B rule is LA bit 0 of the word);
@@ -461,9 +462,9 @@ struct Lane {
     const bool desc = (WIDE ? act : true) && live && !term && !(fc && ahead == 0u);
     const uint32_t push = (desc && avail != 0u) ? 1u : 0u;
     asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %0, 0;\n\t@p st.shared.v4.u32 [%1], {%2, %3, %4, %5};\n\t}"
-                 :: "r"(push), "r"(sp), "r"(ld), "r"(rd), "r"(col), "r"(avail) : "memory");
+                 :: "r"(push), "r"(sp), "r"(ld), "r"(rd), "r"(fr), "r"(avail) : "memory");
     sp += push ? F : 0u;
-    if (desc) { ld = nld; rd = nrd; col = ncol + (1u << 27); avail = nf; }
+    if (desc) { ld = nld; rd = nrd; fr = free_cols; avail = nf; }
   }
 };
 
@@ -479,6 +480,8 @@ __global__ void __launch_bounds__(BLOCK) dfs_kernel(const DfsArgs a) {
   Lane<WIDE, BIG> L;
   L.sbase = L.sp = (uint32_t)__cvta_generic_to_shared(stk);
   const uint32_t sch_sh = (uint32_t)__cvta_generic_to_shared(sch);
+  constexpr uint32_t ROW = BLOCK * (uint32_t)sizeof(W);
+  L.sw0 = sch_sh;                     // a lane without work reads word 0 (fr == 0: no candidate survives)
   uint32_t wexp = 0, job = a.job_base, task = 0;
   bool have = false, exhausted = false;
   unsigned long long acc = 0;
@@ -518,20 +521,25 @@ __global__ void __launch_bounds__(BLOCK) dfs_kernel(const DfsArgs a) {
             L.cnt = (d0 == 0) ? info_root(in.x) : 0u;
             wexp = info_wexp(in.x);
             job = in.y;
-            L.bm = (1u << info_N(in.x)) - 1u;
             L.sp = L.sbase;
             if (T == INFO_NO_DFS || info_status(in.x) != TS_OK || T < d0) {
-              L.avail = 0; L.col = SENT_COL;
+              L.avail = 0; L.fr = 0; L.sw0 = sch_sh;
             } else if ((int)(T - d0) > a.maxt) {    // frames at depths 0..T'-1, words 0..T'
               atomicOr(a.err, DERR_DEPTH);
-              L.avail = 0; L.col = SENT_COL;
+              L.avail = 0; L.fr = 0; L.sw0 = sch_sh;
             } else {
-              L.ld = r.x; L.rd = r.y; L.col = r.z & L.bm; L.avail = r.w;
-              L.tl = T - d0; L.ram = compact_ra_mask((int)info_N(in.x));
+              // root: the free columns of the board, R of them; depth d has R - d (one queen per depth,
+              // T' + 1 <= R of them), so word d is found from popc(fr) alone
+              const uint32_t fr = ((1u << info_N(in.x)) - 1u) & ~r.z;
+              const uint32_t R = __popc(fr);
+              L.ld = r.x; L.rd = r.y; L.fr = fr; L.avail = r.w & fr;
+              L.tf = R - (T - d0); L.sw0 = sch_sh + R * ROW; L.ram = compact_ra_mask((int)info_N(in.x));
               const W* src = gsched + (size_t)task * a.sw + d0;
               for (uint32_t k = 0; k <= T - d0; k++) sch[k * BLOCK] = src[k];
-              // the sentinel under the stack: popped after the last real frame, it leaves no free column
-              stk[0] = make_uint4(0u, 0u, SENT_COL, 0u);
+              // the sentinel under the stack, popped after the last real frame: depth 0 (fr has R
+              // columns, so the word it reads is word 0) with every diagonal blocked, so no
+              // candidate survives
+              stk[0] = make_uint4(~0u, ~0u, fr, 0u);
               L.sp = L.sbase + BLOCK * (uint32_t)sizeof(uint4);
             }
           } else {
@@ -543,7 +551,7 @@ __global__ void __launch_bounds__(BLOCK) dfs_kernel(const DfsArgs a) {
       asm volatile("" ::: "memory");   // refill stores to the schedule before the steps' loads
     }
 #pragma unroll kStepUnroll
-    for (int s = 0; s < kStepsPerCheck; ++s) L.template step<BLOCK>(sch_sh);
+    for (int s = 0; s < kStepsPerCheck; ++s) L.template step<BLOCK>();
   }
 
   const uint32_t j0 = __shfl_sync(FULL, acc_job, 0);
