@@ -1,9 +1,11 @@
 """libnqgpu.so on a CPU-only host: exports, host generator, task schedules.
 
-No kernel runs here.  The schedule tests replay, in Python, the exact
-per-node step of dfs_kernel (nq_kernels.cu) over the schedule words the
-library's own host code derives for each record, and compare the counts
-with the oracle record for record.
+No kernel runs here.  The schedule tests replay, in Python, the per-node
+step of dfs_kernel (nq_kernels.cu) over the schedule words the library's own
+host code derives for each record, and compare the counts with the oracle
+record for record: `replay` in the reference's terms (used columns, an
+explicit depth), `replay_lane` as the kernel's lane runs it (free-column
+frames, depth from their popcount, the sentinel frame).
 """
 import ctypes
 import os
@@ -319,6 +321,101 @@ def test_completion_full_board(nq, oracle_mod):
     t = completion_tasks(4, q)
     assert sum(replay(root, info, w, wide=True)[0] for root, info, w in t) == 1 == oracle_mod.completions(
         4, [r for r, _ in q], [c for _, c in q])
+
+
+def _popc(x):
+    return bin(x).count("1")
+
+
+def replay_lane(root, info, words, wide):
+    """One DFS lane of dfs_kernel as it runs on the GPU: frames {ld, rd, fr, avail} with fr the row's free
+    columns, the depth taken from popc(fr), the child's rows from the funnel shifts of the word with '+' for
+    '|', the terminal test on popc(fr) (compact words), and a sentinel frame {~0, ~0, root fr, 0} under the
+    stack.  Asserts the invariants the kernel relies on: every candidate is a free column and in neither
+    diagonal (so '-' and '+' are exact), and every word the lane reads lies within its schedule.  Returns
+    (weighted count, steps)."""
+    T = info & 31
+    wexp = (info >> 5) & 3
+    cnt = (info >> 7) & 1
+    N = (info >> 8) & 31
+    if T == 31:
+        return cnt << wexp, 0
+    bm = (1 << N) - 1
+    ram = 3 << (N - 1)
+    ld, rd, col, avail = root
+    fr = bm & ~col
+    R = _popc(fr)
+    assert avail & ~fr == 0
+    tf = R - T
+    stack = [(M32, M32, fr, 0)]                 # the sentinel
+    steps = 0
+    while True:
+        if avail == 0:
+            if not stack:
+                break
+            ld, rd, fr, avail = stack.pop()
+        pf = _popc(fr)
+        d = R - pf
+        assert 0 <= d <= T                      # the word read stays inside the lane's schedule
+        act = avail != 0
+        bit = avail & (-avail & M32)
+        avail -= bit
+        if act:
+            steps += 1
+            assert bit & fr and not bit & ld and not bit & rd
+        if wide:
+            x, ra = words[d]
+            s = x & 31
+            nld = ((((ld + bit) & M32) << s) | (x >> (32 - s) if s else 0)) & M32
+            nrd = (((rd + bit) & M32) >> s) | ra
+            term, fc, tall = bool(x & (1 << 6)), bool(x & (1 << 5)), bool(x & (1 << 7))
+        else:
+            w = words[d]
+            s = w & 31
+            nld = ((((ld + bit) & M32) << s) | (w >> (32 - s) if s else 0)) & M32
+            nrd = (((rd + bit) & M32) | (w & ram)) >> s
+            term, fc, tall = pf == tf, bool(w & (1 << 28)), False
+        free = fr - bit
+        nf = free & ~(nld | nrd) & M32
+        ahead = free & ~((((nld + nld) & M32) | (nrd >> 1))) & M32
+        live = nf != 0
+        hit = (act and live and term) or (act and term and tall) if wide else (live and term)
+        cnt += 1 if hit else 0
+        desc = (act if wide else True) and live and not term and not (fc and ahead == 0)
+        if desc and avail:
+            stack.append((ld, rd, fr, avail))
+        if desc:
+            ld, rd, fr, avail = nld, nrd, free, nf
+    return cnt << wexp, steps
+
+
+@pytest.mark.parametrize("N,preset", [(n, p) for n in range(6, 12) for p in (4, 5, 6, 7)] + [(12, 5), (13, 6)])
+def test_lane_replay_matches_oracle(nq, oracle_mod, N, preset):
+    """The kernel's lane state machine (free-column frames) gives every record's count, visits the same
+    steps as the reference-semantics replay, and keeps its invariants."""
+    try:
+        o = oracle_mod.gen_constellations(N, preset)
+        if len(o) == 0:
+            return
+        sol = oracle_mod.exec_solutions(N, o, threads=1)
+    except ValueError:
+        pytest.skip("the reference raises for this preset (negative shift)")
+    rec = np.zeros(len(o), nq.RECORD_DTYPE)
+    rec["ld"] = o.ld & M32; rec["rd"] = o.rd & M32; rec["col"] = o.col & M32; rec["startijkl"] = o.startijkl
+    for i in range(len(o)):
+        root, info, words = schedule_of(rec[i], N)
+        got, steps = replay_lane(root, info, words, wide=False)
+        assert got == int(sol[i]), (i, rec[i])
+        assert steps == replay(root, info, words, wide=False)[1]
+
+
+@pytest.mark.parametrize("N", range(4, 11))
+def test_lane_replay_of_completion_tasks(nq, oracle_mod, N):
+    rng = np.random.default_rng(2000 + N)
+    for q in [[]] + [random_queens(rng, N, k) for k in (1, 2, 2, 3) if k < N]:
+        want = oracle_mod.completions(N, [r for r, _ in q], [c for _, c in q])
+        got = sum(replay_lane(root, info, w, wide=True)[0] for root, info, w in completion_tasks(N, q))
+        assert got == want, (N, q)
 
 
 def test_exec_solutions_rejects_cpu_path(nq):
