@@ -156,6 +156,14 @@ int nq_count(nq_handle *h, int N, int preset, uint64_t *total);
  * out != NULL and cap is large enough; returns their number or a negative
  * status.  Host only. */
 int64_t nq_start_constellations(int N, int32_t *out, int64_t cap);
+/* The records that start constellations [first, first + count) of
+ * nq_start_constellations' list expand into (preset <= 0: nq_preset_for(N)),
+ * in the order nq_gen_constellations lists them: the per-start loop of the
+ * reference's streamed task writer (gen_constellations_stream_to_bin,
+ * 356Py_savesp_narrow.py:2988-3084), a range at a time.  Writes them when
+ * out != NULL and cap is large enough; returns their number or a negative
+ * status (a range outside the list is NQ_EINVAL).  Host only. */
+int64_t nq_gen_constellations_starts(int N, int preset, int64_t first, int64_t count, nq_record *out, int64_t cap);
 /* The part of nq_count(N, preset) that comes from start constellations
  * [first, first + count) of nq_start_constellations' list: the records those
  * starts expand into (preset <= 0: nq_preset_for(N)), streamed the same way.

@@ -583,6 +583,25 @@ int64_t nq_start_constellations(int N, int32_t* out, int64_t cap) {
   return n;
 }
 
+int64_t nq_gen_constellations_starts(int N, int preset, int64_t first, int64_t count, nq_record* out, int64_t cap) {
+  if (N < 6 || N > kMaxN) return NQ_EINVAL;
+  const int p = preset > 0 ? preset : preset_for(N);
+  if (p < 4) return NQ_EPRESET;
+  std::vector<int> starts;
+  if (start_constellations(N, starts) != 0) return NQ_EINVAL;
+  const int64_t ns = (int64_t)starts.size();
+  if (first < 0 || count < 0 || first > ns || count > ns - first) return NQ_EINVAL;
+  std::vector<GenRecord> v;
+  const int e = expand_starts(N, p, starts, (size_t)first, (size_t)(first + count), v, 0);
+  if (e == -1) return NQ_EINVAL;
+  if (e == -2) return NQ_EPRESET;
+  const int64_t n = (int64_t)v.size();
+  if (out && cap >= n)
+    for (int64_t i = 0; i < n; i++)
+      out[i] = nq_record{(uint32_t)v[i].ld, (uint32_t)v[i].rd, (uint32_t)v[i].col, v[i].startijkl};
+  return n;
+}
+
 int nq_count_starts(nq_handle* h, int N, int preset, int64_t first, int64_t count, uint64_t* total) {
   if (!h || !total) return NQ_EINVAL;
   if (N < 6 || N > kMaxN) return h->fail(NQ_EINVAL, "count_starts: N=%d outside 6..27", N);

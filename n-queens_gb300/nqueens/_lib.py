@@ -79,6 +79,8 @@ SIGNATURES = {
     "nq_last_kernel_ms": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
     "nq_count": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _u64p]),
     "nq_start_constellations": (ctypes.c_int64, [ctypes.c_int, _vp, ctypes.c_int64]),
+    "nq_gen_constellations_starts": (ctypes.c_int64, [ctypes.c_int, ctypes.c_int, ctypes.c_int64, ctypes.c_int64, _vp,
+                                                     ctypes.c_int64]),
     "nq_count_starts": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int64, ctypes.c_int64, _u64p]),
     "nq_set_chunk_records": (ctypes.c_int, [_vp, ctypes.c_int64]),
     "nq_last_count_info": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]),

@@ -20,6 +20,10 @@ chunks already there, so a count too long for one run is finished by rerunning
 the same command (--stop-after C ends a run after C new chunks, --time-limit S
 before a chunk that would end past S seconds).
 
+--write-tasks FILE with --n (and --preset) writes the board's task list as the
+reference's constellations_N{N}_{P}.bin with its .done sidecar, streamed a block
+of start constellations at a time (host only, no GPU).
+
 --tasks counts one of the reference's cached task files (16-byte records,
 N taken from the file name or --n) and --write-solutions writes the
 per-record counts as the reference's 40-byte solutions_*_v2.bin cache.  The
@@ -116,6 +120,18 @@ def _count_with_progress(a) -> int:
     return 0 if status == "ok" else 1
 
 
+def _write_tasks(a) -> int:
+    from . import formats
+    N = a.n
+    if not 6 <= N <= 27:
+        print("--write-tasks needs --n (6..27)", file=sys.stderr)
+        return 2
+    t0 = dt.datetime.now()
+    n = formats.stream_tasks(a.write_tasks, N, a.preset or None)
+    print(f"{a.write_tasks}: N={N} records={n} {_fmt(dt.datetime.now() - t0)}")
+    return 0
+
+
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser(prog="python -m nqueens", description=__doc__.split("\n")[0])
     ap.add_argument("nmin", nargs="?", type=int, default=5)
@@ -132,13 +148,16 @@ def main(argv=None) -> int:
     ap.add_argument("--regenerate", action="store_true",
                     help="with --n: generate the constellations (full-width masks) instead of reading --tasks")
     ap.add_argument("--preset", type=int, default=0,
-                    help="with --regenerate or --progress: preset queens (0: the dynamic preset)")
+                    help="with --regenerate, --progress or --write-tasks: preset queens (0: the dynamic preset)")
+    ap.add_argument("--write-tasks", help="with --n: write the task list to this .bin file (no count)")
     ap.add_argument("--progress", help="count board nmin resumably, keeping per-chunk totals in this file")
     ap.add_argument("--chunk-starts", type=int, default=64, help="with --progress: start constellations per chunk")
     ap.add_argument("--stop-after", type=int, default=None, help="with --progress: stop after this many new chunks")
     ap.add_argument("--time-limit", type=float, default=None,
                     help="with --progress: start no chunk that would end past this many seconds")
     a = ap.parse_args(argv)
+    if a.write_tasks:
+        return _write_tasks(a)
     if a.progress:
         return _count_with_progress(a)
     if a.regenerate:

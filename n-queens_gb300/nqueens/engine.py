@@ -78,6 +78,21 @@ def start_constellations(N: int) -> np.ndarray:
     return out
 
 
+def gen_records_starts(N: int, first: int, count: int, preset: Optional[int] = None) -> np.ndarray:
+    """Records (RECORD_DTYPE) that start constellations [first, first+count) of start_constellations(N)
+    expand into, in gen_records' order: concatenated over a partition of the list they are gen_records(N)."""
+    p = select_dynamic_preset_queens(N) if preset is None else int(preset)
+    L = lib()
+    n = L.nq_gen_constellations_starts(int(N), p, int(first), int(count), None, 0)
+    if n < 0:
+        _check(int(n), what=f"gen_constellations_starts(N={N}, {first}, {count}, preset={p})")
+    out = np.zeros(n, RECORD_DTYPE)
+    if n and L.nq_gen_constellations_starts(int(N), p, int(first), int(count), out.ctypes.data_as(ctypes.c_void_p),
+                                            n) != n:
+        raise NQError(_lib.NQ_EINVAL, "generator returned a different count on the second call")
+    return out
+
+
 def gen_records_wide(N: int, preset: Optional[int] = None) -> Tuple[np.ndarray, np.ndarray, np.ndarray, np.ndarray]:
     """(ld, rd, col, startijkl) with the reference's full-width masks (uint64, uint64, uint64, uint32)."""
     p = select_dynamic_preset_queens(N) if preset is None else int(preset)

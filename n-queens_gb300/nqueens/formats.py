@@ -12,6 +12,15 @@
 
 These files let the engine consume the reference's cached task lists and write
 solution files the reference can load.  Corrupt inputs raise ``FormatError``.
+
+``stream_tasks`` writes a task list the way the reference's streamed writer does
+(``gen_constellations_stream_to_bin``, 356Py:2988-3084): the file is truncated
+and its ``.done`` set to 0, the records of a block of start constellations at a
+time are appended, and ``.done`` gets the record count only once the file is
+complete, so host memory stays bounded by one block at the largest boards.
+``ensure_tasks`` is its cache check (``ensure_constellations_bin_stream``,
+:3086-3102): a file whose ``.done`` matches its size is reused, any other is
+rebuilt.
 """
 from __future__ import annotations
 
@@ -111,3 +120,38 @@ def fill_from_solutions(constellations: List[dict], sol: np.ndarray) -> Optional
             return key
         c["solutions"] = mp[key]
     return None
+
+
+def stream_tasks(path: str, N: int, preset: Optional[int] = None, starts_per_block: int = 256) -> int:
+    """Write the task list of N (preset None: the dynamic preset) to path block by block of start
+    constellations; returns the record count.  The file's bytes equal save_tasks(path, gen_records(N))."""
+    from .engine import gen_records_starts, start_constellations
+    if starts_per_block < 1:
+        raise ValueError("starts_per_block must be >= 1")
+    n_starts = len(start_constellations(N))
+    with open(path, "wb"):
+        pass
+    write_done(path + ".done", 0)
+    total = 0
+    with open(path, "ab") as f:
+        for a in range(0, n_starts, starts_per_block):
+            recs = gen_records_starts(N, a, min(starts_per_block, n_starts - a), preset)
+            recs.tofile(f)
+            total += len(recs)
+        f.flush()
+        os.fsync(f.fileno())
+    write_done(path + ".done", total)
+    return total
+
+
+def ensure_tasks(N: int, preset: Optional[int] = None, directory: str = ".", starts_per_block: int = 256) -> str:
+    """Path of a complete task file constellations_N{N}_{P}.bin in directory, written by stream_tasks
+    unless a complete one (``.done`` equal to its record count) is already there."""
+    from .engine import select_dynamic_preset_queens
+    p = select_dynamic_preset_queens(N) if preset is None else int(preset)
+    path = os.path.join(directory, task_file_name(N, p))
+    size = os.path.getsize(path) if os.path.exists(path) else -1
+    if size > 0 and size % 16 == 0 and read_done(path + ".done") == size // 16:
+        return path
+    stream_tasks(path, N, p, starts_per_block)
+    return path

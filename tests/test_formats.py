@@ -95,3 +95,64 @@ def test_cli_counts_a_task_file_and_writes_solutions(tmp_path, oracle_mod, capsy
     want = oracle_mod.exec_solutions(N, oracle_mod.Records(recs["ld"].astype(np.uint64), recs["rd"].astype(np.uint64),
                                                            recs["col"].astype(np.uint64), recs["startijkl"].copy()))
     assert np.array_equal(sol["solutions"], want) and np.array_equal(sol["startijkl"], recs["startijkl"])
+
+
+@pytest.mark.parametrize("N,block", [(9, 1), (13, 100), (16, 256), (19, 4096)])
+def test_streamed_task_file_matches_archive(tmp_path, N, block):
+    """The streamed writer appends a block of start constellations at a time; the finished file holds the
+    same bytes as the whole list written at once, its .done the record count, and its records the
+    reference's archived task list (digest of constellations_N{N}_5.bin)."""
+    import nqueens
+    from nqueens import formats
+    d = json.load(open(os.path.join(GOLDEN, "archive_digests.json")))["tasks"]
+    p = str(tmp_path / formats.task_file_name(N, 5))
+    n = formats.stream_tasks(p, N, 5, starts_per_block=block)
+    back = formats.load_tasks(p, require_done=True)
+    assert n == len(back) == d[str(N)]["records"]
+    assert task_digest(back["startijkl"], back["ld"], back["rd"], back["col"]) == d[str(N)]["sha256"]
+    assert open(p, "rb").read() == nqueens.gen_records(N, 5).tobytes()
+
+
+def test_records_of_start_ranges_partition_the_task_list():
+    import nqueens
+    N = 14
+    n = len(nqueens.start_constellations(N))
+    cuts = [0, 1, 2, 50, 51, 900, n]
+    parts = [nqueens.gen_records_starts(N, a, b - a) for a, b in zip(cuts[:-1], cuts[1:])]
+    assert np.concatenate(parts).tobytes() == nqueens.gen_records(N).tobytes()
+    assert len(nqueens.gen_records_starts(N, n, 0)) == 0
+    for a, c in [(-1, 1), (0, n + 1), (n, 1)]:
+        with pytest.raises(nqueens.NQError):
+            nqueens.gen_records_starts(N, a, c)
+    with pytest.raises(nqueens.NQError):
+        nqueens.gen_records_starts(N, 0, 5, preset=3)
+
+
+def test_ensure_tasks_reuses_a_complete_file_and_rebuilds_others(tmp_path):
+    import nqueens
+    from nqueens import formats
+    N = 12
+    p = formats.ensure_tasks(N, 5, str(tmp_path))
+    assert os.path.basename(p) == "constellations_N12_5.bin"
+    want = nqueens.gen_records(N, 5).tobytes()
+    assert open(p, "rb").read() == want
+    mtime = os.stat(p).st_mtime_ns
+    assert formats.ensure_tasks(N, 5, str(tmp_path)) == p and os.stat(p).st_mtime_ns == mtime   # cache hit
+    with open(p, "r+b") as f:                                  # an interrupted write: shorter than .done says
+        f.truncate(16 * 10)
+    formats.ensure_tasks(N, 5, str(tmp_path))
+    assert open(p, "rb").read() == want
+    formats.write_done(p + ".done", 0)                          # a writer that never finished
+    formats.ensure_tasks(N, 5, str(tmp_path))
+    assert formats.read_done(p + ".done") == len(want) // 16
+
+
+def test_cli_writes_a_task_file(tmp_path, capsys):
+    import nqueens
+    from nqueens import formats
+    from nqueens.cli import main
+    p = str(tmp_path / "constellations_N13_6.bin")
+    assert main(["--write-tasks", p, "--n", "13", "--preset", "6"]) == 0
+    assert "records=" in capsys.readouterr().out
+    assert np.array_equal(formats.load_tasks(p, require_done=True), nqueens.gen_records(13, 6))
+    assert main(["--write-tasks", p]) == 2
