@@ -430,3 +430,15 @@ def test_cli_progress_resumes(tmp_path, capsys):
     assert "stopped" in capsys.readouterr().out
     assert main(["15", "16", "--progress", p, "--chunk-starts", "300"]) == 0
     assert "2279184" in capsys.readouterr().out
+
+
+def test_board_sharded_by_start_ranges_on_gpu(eng, oracle_mod):
+    """Whole-board counts split over ranks by start-constellation chunks: one rank alone, and three ranks'
+    chunk lists counted in turn on this GPU, give the known total."""
+    import nqueens
+    from nqueens.shard import board_chunks, count_board_sharded
+    N = 17
+    assert count_board_sharded(N, 0, 1, chunk=500, engine=eng) == oracle_mod.EXPECTED_TOTAL[N]
+    n = len(nqueens.start_constellations(N))
+    parts = [sum(eng.count_starts(N, a, c) for a, c in board_chunks(n, 300, r, 3)) for r in range(3)]
+    assert sum(parts) == oracle_mod.EXPECTED_TOTAL[N] and min(parts) > 0
