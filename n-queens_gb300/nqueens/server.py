@@ -60,7 +60,7 @@ class _InFlight:
 # GPU milliseconds of a whole-board count, the starting point of each server's table: measured on
 # GB300 with bench-style timing; a server replaces an entry with the run time it measures for a
 # single-request batch of that board (exponential average), so another GPU recalibrates itself.
-_COUNT_MS = {16: 0.9, 17: 3.0, 18: 16.0, 19: 108.0, 20: 860.0, 21: 7300.0}
+_COUNT_MS = {16: 0.5, 17: 2.2, 18: 13.0, 19: 86.0, 20: 670.0, 21: 5600.0}
 
 
 def estimate_ms(job, table: Optional[dict] = None) -> float:

@@ -195,4 +195,4 @@ def test_timing_table_recalibrates_from_measured_batches(fake):
         assert s._count_ms[16] == srv_mod._COUNT_MS[16]
         s.submit(nqueens.CountJob(16)).result(timeout=30)
         s.drain(30)
-        assert s._count_ms[16] > 10 * srv_mod._COUNT_MS[16]   # the fake's 50 ms run replaced the GB300 0.9 ms
+        assert s._count_ms[16] > 10 * srv_mod._COUNT_MS[16]   # the fake's 50 ms run replaced the GB300 entry
